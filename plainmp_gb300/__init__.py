@@ -1,0 +1,15 @@
+"""plainmp_gb300: GB300-native collision-checking hot path of plainmp.
+
+Batched forward kinematics, sphere-vs-SDF checks (box, sphere, cylinder, ground, point
+cloud), self-collision sphere pairs, motion-validator edge checks and constraint Jacobians,
+as hand-written sm_103a CUDA kernels behind the C ABI in include/pmgpu.h.  The Python
+modules mirror the reference's ``plainmp.kinematics``, ``plainmp.psdf`` and
+``plainmp.constraint`` interfaces.
+"""
+from ._lib import CudaError, DeviceTimeout, device_count  # noqa: F401
+from .constraint import SphereAttachmentSpec, SphereCollisionCst  # noqa: F401
+from .kinematics import BaseType, KinematicModel  # noqa: F401
+from .motion_validator import BoxMotionValidator, EuclideanMotionValidator  # noqa: F401
+from .psdf import BoxSDF, CloudSDF, CylinderSDF, GroundSDF, Pose, SDFBase, SphereSDF, UnionSDF  # noqa: F401
+
+__version__ = "0.1.0"

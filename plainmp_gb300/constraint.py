@@ -1,0 +1,191 @@
+"""SphereCollisionCst mirroring plainmp.constraint (src/plainmp/constraint.pyi:9-38,76-94,
+cpp/plainmp/bindings/constraint.cpp:65-84) on top of the C ABI.
+
+Single-configuration methods keep the reference's signatures (``is_valid(q) -> bool``,
+``evaluate(q) -> (vals, jac)``, ``update_kintree(q, high_accuracy)``); the ``*_batch``
+methods take a (B, q_dim) numpy array (host memory) or a torch CUDA tensor (device memory,
+enqueued on torch's current stream) and are the GB300 hot path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from ._lib import Batch, check, cstrs, dptr, f64, lib
+from .kinematics import BaseType, KinematicModel
+from .psdf import SDFBase
+
+
+@dataclass
+class SphereAttachmentSpec:
+    """SphereAttachmentSpec(parent_link_name, relative_positions (3, n), radii (n,), only_self_collision)."""
+
+    parent_link_name: str
+    relative_positions: np.ndarray
+    radii: np.ndarray
+    only_self_collision: bool = False
+
+    def __post_init__(self):
+        self.relative_positions = f64(self.relative_positions)
+        self.radii = f64(self.radii).reshape(-1)
+        if self.relative_positions.ndim != 2 or self.relative_positions.shape[0] != 3:
+            raise ValueError("relative_positions must be (3, n)")
+        if self.relative_positions.shape[1] != self.radii.shape[0]:
+            raise ValueError("relative_positions and radii disagree on the sphere count")
+
+
+class SphereCollisionCst:
+    def __init__(self, kin: KinematicModel, control_joint_names: Sequence[str], base_type: BaseType,
+                 sphere_specs: Sequence[SphereAttachmentSpec], selcol_pairs: Sequence[Tuple[str, str]],
+                 fixed_sdf: Optional[SDFBase] = None, reorder_spheres: bool = True) -> None:
+        self._kin = kin
+        self._fixed = fixed_sdf
+        self._sdf = None
+        self.control_joint_names = list(control_joint_names)
+        self.base_type = BaseType(int(base_type))
+        counts = np.array([s.radii.shape[0] for s in sphere_specs], dtype=np.int32)
+        rel = (np.concatenate([s.relative_positions.T for s in sphere_specs], axis=0) if sphere_specs else np.zeros((0, 3)))
+        rel = f64(rel)
+        radii = f64(np.concatenate([s.radii for s in sphere_specs]) if sphere_specs else np.zeros(0))
+        only = np.array([1 if s.only_self_collision else 0 for s in sphere_specs], dtype=np.uint8)
+        h = C.c_void_p()
+        check(lib.pmgpu_cst_create(
+            kin._h, cstrs(self.control_joint_names), len(self.control_joint_names), int(self.base_type),
+            len(sphere_specs), cstrs([s.parent_link_name for s in sphere_specs]),
+            counts.ctypes.data_as(C.POINTER(C.c_int32)), dptr(rel), dptr(radii), only.ctypes.data_as(C.POINTER(C.c_uint8)),
+            len(selcol_pairs), cstrs([a for a, _ in selcol_pairs]), cstrs([b for _, b in selcol_pairs]),
+            fixed_sdf._h if fixed_sdf is not None else None, int(bool(reorder_spheres)), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.pmgpu_cst_destroy(h)
+            self._h = None
+
+    # ---- structure
+    def _dims(self):
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(lib.pmgpu_cst_dims(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return a.value, b.value, c.value, d.value
+
+    def q_dim(self) -> int:
+        return self._dims()[0]
+
+    def cst_dim(self) -> int:
+        return self._dims()[1]
+
+    @property
+    def n_spheres(self) -> int:
+        return self._dims()[2]
+
+    @property
+    def n_groups(self) -> int:
+        return self._dims()[3]
+
+    def groups(self) -> dict:
+        """Constructed group table (post-reorder order)."""
+        ng, ns = self.n_groups, self.n_spheres
+        i32 = C.POINTER(C.c_int32)
+        link = np.empty(max(ng, 1), dtype=np.int32)
+        rad = np.empty(max(ng, 1))
+        ctr = np.empty((max(ng, 1), 3))
+        only = np.empty(max(ng, 1), dtype=np.int32)
+        rel = np.empty((max(ns, 1), 3))
+        sr = np.empty(max(ns, 1))
+        check(lib.pmgpu_cst_groups(self._h, link.ctypes.data_as(i32), dptr(rad), dptr(ctr), only.ctypes.data_as(i32), dptr(rel), dptr(sr)))
+        return {"link": link[:ng], "radius": rad[:ng], "centre": ctr[:ng], "only_self": only[:ng], "rel": rel[:ns], "radii": sr[:ns]}
+
+    def get_kin(self) -> KinematicModel:
+        return self._kin
+
+    def get_control_joint_names(self) -> List[str]:
+        return list(self.control_joint_names)
+
+    def set_sdf(self, sdf: Optional[SDFBase]) -> None:
+        check(lib.pmgpu_cst_set_sdf(self._h, sdf._h if sdf is not None else None))
+        self._sdf = sdf
+
+    def get_sdf(self) -> Optional[SDFBase]:
+        return self._sdf
+
+    # ---- single configuration (reference signatures)
+    def update_kintree(self, q, high_accuracy: bool = True) -> None:
+        qq = f64(q, (self.q_dim(),))
+        check(lib.pmgpu_cst_update_kintree(self._h, dptr(qq), int(bool(high_accuracy))))
+
+    def is_valid(self, q) -> bool:
+        """IneqConstraintBase.is_valid: also leaves the model in q's state, as the reference does."""
+        qq = f64(q, (1, self.q_dim()))
+        ok = bool(self.is_valid_batch(qq)[0])
+        self.update_kintree(qq[0], high_accuracy=self.base_type != BaseType.FIXED)
+        return ok
+
+    def evaluate(self, q) -> Tuple[np.ndarray, np.ndarray]:
+        qq = f64(q, (1, self.q_dim()))
+        vals, jac = self.evaluate_batch(qq)
+        self.update_kintree(qq[0], high_accuracy=True)
+        return vals[0], jac[0]
+
+    def get_all_spheres(self) -> List[Tuple[np.ndarray, float]]:
+        n = self.n_spheres
+        out = np.empty((max(n, 1), 4))
+        check(lib.pmgpu_cst_get_all_spheres(self._h, dptr(out)))
+        return [(out[i, :3].copy(), float(out[i, 3])) for i in range(n)]
+
+    def get_group_spheres(self) -> List[Tuple[np.ndarray, float]]:
+        n = self.n_groups
+        out = np.empty((max(n, 1), 4))
+        check(lib.pmgpu_cst_get_group_spheres(self._h, dptr(out)))
+        return [(out[i, :3].copy(), float(out[i, 3])) for i in range(n)]
+
+    # ---- batches (the device hot path)
+    def _batch(self, Q):
+        b = Batch(Q)
+        if len(b.shape) != 2 or b.shape[1] != self.q_dim():
+            raise ValueError(f"expected a (B, {self.q_dim()}) batch, got {b.shape}")
+        return b
+
+    def is_valid_batch(self, Q):
+        """Plain FP64 method: (B,) uint8 validity, bit-exact with the reference."""
+        b = self._batch(Q)
+        out, optr = b.empty((b.shape[0],), np.uint8)
+        check(lib.pmgpu_cst_is_valid(self._h, b.ptr, b.shape[0], optr, b.mem, b.stream))
+        return out
+
+    def evaluate_batch(self, Q):
+        """(vals (B, cst_dim), jac (B, cst_dim, q_dim)) in FP64."""
+        b = self._batch(Q)
+        m, d = self.cst_dim(), self.q_dim()
+        vals, vptr = b.empty((b.shape[0], m), np.float64)
+        jac, jptr = b.empty((b.shape[0], m, d), np.float64)
+        check(lib.pmgpu_cst_evaluate(self._h, b.ptr, b.shape[0], vptr, jptr, b.mem, b.stream))
+        return vals, jac
+
+    def sphere_distances(self, Q, high_accuracy: bool = False, centres: bool = False):
+        """Per-sphere signed distance (B, n_spheres) in FP64 (and centres (B, n_spheres, 3))."""
+        b = self._batch(Q)
+        ns = self.n_spheres
+        dist, dptr_ = b.empty((b.shape[0], ns), np.float64)
+        cen, cptr = b.empty((b.shape[0], ns, 3), np.float64) if centres else (None, None)
+        check(lib.pmgpu_cst_sphere_distances(self._h, b.ptr, b.shape[0], int(bool(high_accuracy)), dptr_, cptr, b.mem, b.stream))
+        return (dist, cen) if centres else dist
+
+    def is_valid_fast(self, Q, distances: bool = False, stats: bool = False):
+        """FP32 + FP64-recheck path: validity identical to is_valid_batch; optional FP32
+        per-sphere distances (B, n_spheres) and recheck statistics."""
+        b = self._batch(Q)
+        out, optr = b.empty((b.shape[0],), np.uint8)
+        dist, dp = b.empty((b.shape[0], self.n_spheres), np.float32) if distances else (None, None)
+        st = np.zeros(4, dtype=np.int64)
+        check(lib.pmgpu_cst_is_valid_fast(self._h, b.ptr, b.shape[0], optr, dp, C.c_void_p(st.ctypes.data) if stats else None,
+                                          b.mem, b.stream))
+        res = [out]
+        if distances:
+            res.append(dist)
+        if stats:
+            res.append({"configs": int(st[0]), "rechecked_terms": int(st[1]), "rechecked_configs": int(st[2])})
+        return res[0] if len(res) == 1 else tuple(res)

@@ -1,0 +1,1552 @@
+// Host side of the drop-in boundary: KinematicModel, primitive SDFs and SphereCollisionCst
+// objects, their flattening into device tables, and the extern "C" entry points of
+// include/pmgpu.h.  Construction-time bookkeeping (URDF tree numbering, pose flags, AABBs,
+// sphere-group statistics) runs here as it does in the reference's constructors; every
+// per-configuration computation runs on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "host_urdf.h"
+#include "pm_common.h"
+#include "pm_launch.h"
+#include "pmgpu.h"
+
+namespace pmg {
+
+// ---------------------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+struct PmError : std::runtime_error {
+  int code;
+  PmError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+[[noreturn]] static void fail(int code, const std::string& msg) { throw PmError(code, msg); }
+static void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(PMGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    f();
+    g_last_error.clear();
+    return PMGPU_OK;
+  } catch (const PmError& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::invalid_argument& e) {
+    g_last_error = e.what();
+    return PMGPU_ERR_INVALID;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return PMGPU_ERR_RUNTIME;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return PMGPU_ERR_RUNTIME;
+  }
+}
+
+static void require_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    fail(PMGPU_ERR_CUDA, "no CUDA device available: the GB300 kernels cannot run on this host");
+  }
+}
+
+// ---------------------------------------------------------------------------- device buffers
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void* ensure(size_t bytes) {
+    if (bytes <= n && p) return p;
+    release();
+    size_t b = std::max<size_t>(bytes, 256);
+    cuda_check(cudaMalloc(&p, b), "cudaMalloc");
+    n = b;
+    return p;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+// ---------------------------------------------------------------------------- host quaternion
+// construction-time helpers (setQuaternionFromRPY, transform.hpp:122-130)
+static void quat_from_rpy(double r, double p, double y, double q[4]) {
+  double phi = r / 2.0, the = p / 2.0, psi = y / 2.0;
+  q[0] = std::sin(phi) * std::cos(the) * std::cos(psi) - std::cos(phi) * std::sin(the) * std::sin(psi);
+  q[1] = std::cos(phi) * std::sin(the) * std::cos(psi) + std::sin(phi) * std::cos(the) * std::sin(psi);
+  q[2] = std::cos(phi) * std::cos(the) * std::sin(psi) - std::sin(phi) * std::sin(the) * std::cos(psi);
+  q[3] = std::cos(phi) * std::cos(the) * std::cos(psi) + std::sin(phi) * std::sin(the) * std::sin(psi);
+}
+
+// ---------------------------------------------------------------------------- KinematicModel
+struct HostJoint {
+  std::string name;
+  int type;  // UrdfJointType
+  int child;
+  double axis[3], pos[3], quat[4];
+  bool qid;
+  double lower, upper;
+};
+
+struct HostModel {
+  std::vector<std::string> link_name;
+  std::map<std::string, int> link_id;
+  std::vector<int> parent;
+  std::vector<std::vector<int>> children;
+  std::vector<char> consider_rotation;
+  std::vector<HostJoint> joints;
+  std::map<std::string, int> joint_id;
+  std::vector<int> link_parent_joint;  // movable joint id owning the link, -1 otherwise
+  int root = 0;
+  std::vector<double> state_init;  // rows of PM_STATE_STRIDE doubles (row 0 = base)
+  std::vector<double> angles;
+  double base7[7] = {0, 0, 0, 0, 0, 0, 1};
+  uint64_t version = 1;  // bumped when the link set changes
+  // device
+  DevBuf d_state;
+  DevBuf d_parents;
+  DevBuf d_scratch;
+  int dev_rows = 0;
+  bool dev_ready = false;
+
+  int n_link() const { return (int)link_name.size(); }
+
+  void ensure_device() {
+    if (dev_ready && dev_rows == n_link() + 1) return;
+    require_device();
+    size_t rows = n_link() + 1;
+    std::vector<double> host(state_init);
+    if (dev_ready && dev_rows > 0) {  // keep the current state when links were appended
+      std::vector<double> old((size_t)dev_rows * PM_STATE_STRIDE);
+      cuda_check(cudaMemcpy(old.data(), d_state.p, old.size() * 8, cudaMemcpyDeviceToHost), "state readback");
+      std::copy(old.begin(), old.end(), host.begin());
+      d_state.release();
+    }
+    d_state.ensure(rows * PM_STATE_STRIDE * 8);
+    cuda_check(cudaMemcpy(d_state.p, host.data(), rows * PM_STATE_STRIDE * 8, cudaMemcpyHostToDevice), "state upload");
+    std::vector<int32_t> par(parent.begin(), parent.end());
+    d_parents.release();
+    d_parents.ensure(par.size() * 4);
+    cuda_check(cudaMemcpy(d_parents.p, par.data(), par.size() * 4, cudaMemcpyHostToDevice), "parents upload");
+    dev_rows = (int)rows;
+    dev_ready = true;
+  }
+};
+
+static void set_row(std::vector<double>& st, int row, const double q[4], const double t[3], bool qid) {
+  double* r = st.data() + (size_t)row * PM_STATE_STRIDE;
+  r[0] = q[0];
+  r[1] = q[1];
+  r[2] = q[2];
+  r[3] = q[3];
+  r[4] = t[0];
+  r[5] = t[1];
+  r[6] = t[2];
+  r[7] = qid ? 1.0 : 0.0;
+}
+
+// KinematicModel ctor (kinematics.cpp:183-223): stack-DFS link numbering, stack-DFS numbering
+// of movable joints, local transforms from joint origins, identity flags.
+static std::shared_ptr<HostModel> build_model(const std::string& xml) {
+  UrdfRobot r = parse_urdf(xml);
+  auto m = std::make_shared<HostModel>();
+  std::map<std::string, std::vector<std::string>> child_links;
+  for (auto& kv : r.child_joints)
+    for (auto& jn : kv.second) child_links[kv.first].push_back(r.joints.at(jn).child);
+  std::vector<std::string> order;
+  std::vector<std::string> st{r.root};
+  while (!st.empty()) {
+    std::string l = st.back();
+    st.pop_back();
+    m->link_id[l] = (int)order.size();
+    order.push_back(l);
+    for (auto& c : child_links[l]) st.push_back(c);
+  }
+  int nl = (int)order.size();
+  if (nl != (int)r.links.size()) fail(PMGPU_ERR_RUNTIME, "URDF: the links do not form one tree");
+  m->link_name = order;
+  m->parent.assign(nl, -1);
+  m->children.resize(nl);
+  m->consider_rotation.assign(nl, 1);
+  m->link_parent_joint.assign(nl, -1);
+  for (int i = 0; i < nl; i++) {
+    auto pj = r.parent_joint.find(order[i]);
+    if (pj != r.parent_joint.end()) m->parent[i] = m->link_id[r.joints.at(pj->second).parent];
+    for (auto& c : child_links[order[i]]) m->children[i].push_back(m->link_id[c]);
+  }
+  m->root = 0;
+  // joints (kinematics.cpp:66-145)
+  std::vector<std::string> jst;
+  for (auto& jn : r.child_joints[r.root]) jst.push_back(jn);
+  while (!jst.empty()) {
+    const UrdfJoint& j = r.joints.at(jst.back());
+    jst.pop_back();
+    if (j.type == UJ_REVOLUTE || j.type == UJ_CONTINUOUS || j.type == UJ_PRISMATIC) {
+      HostJoint h;
+      h.name = j.name;
+      h.type = j.type;
+      h.child = m->link_id[j.child];
+      std::memcpy(h.axis, j.axis, sizeof(h.axis));
+      std::memcpy(h.pos, j.xyz, sizeof(h.pos));
+      std::memcpy(h.quat, j.quat, sizeof(h.quat));
+      h.qid = std::abs(h.quat[3] - 1.0) < 1e-6;
+      if (j.type == UJ_CONTINUOUS) {
+        h.lower = -std::numeric_limits<double>::infinity();
+        h.upper = std::numeric_limits<double>::infinity();
+      } else {
+        h.lower = j.lower;
+        h.upper = j.upper;
+      }
+      m->joint_id[h.name] = (int)m->joints.size();
+      m->link_parent_joint[h.child] = (int)m->joints.size();
+      m->joints.push_back(h);
+    }
+    auto cj = r.child_joints.find(j.child);
+    if (cj != r.child_joints.end())
+      for (auto& jn : cj->second) jst.push_back(jn);
+  }
+  m->angles.assign(m->joints.size(), 0.0);
+  // state rows: base = Transform::Identity(); links = joint origin transforms (kinematics.cpp:147-181)
+  m->state_init.assign((size_t)(nl + 1) * PM_STATE_STRIDE, 0.0);
+  const double qi[4] = {0, 0, 0, 1}, z3[3] = {0, 0, 0};
+  set_row(m->state_init, PM_STATE_BASE_ROW, qi, z3, false);
+  for (int i = 0; i < nl; i++) {
+    auto pj = r.parent_joint.find(order[i]);
+    if (pj == r.parent_joint.end()) {  // the root's local transform is never composed
+      set_row(m->state_init, PM_STATE_LINK_ROW(i), qi, z3, false);
+      continue;
+    }
+    const UrdfJoint& j = r.joints.at(pj->second);
+    set_row(m->state_init, PM_STATE_LINK_ROW(i), j.quat, j.xyz, std::abs(j.quat[3] - 1.0) < 1e-6);
+  }
+  return m;
+}
+
+// ---------------------------------------------------------------------------- SDFs
+static std::atomic<uint64_t> g_sdf_version{1};
+
+struct CloudData {
+  GridBuild g{};
+  DevBuf d_grid;  // one PmGridDev on the device
+  std::vector<double> pts;
+  double radius = 0;
+  double cell = 0;
+  double lb[3], ub[3];
+  bool built = false;
+  ~CloudData() {
+    if (built) grid_free(g);
+  }
+};
+
+struct HostSdf {
+  int kind = PM_SDF_BOX;
+  uint64_t version = 0;
+  double lb[3] = {0, 0, 0}, ub[3] = {0, 0, 0};
+  double pos[3] = {0, 0, 0};
+  double rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  double rot_inv[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  bool axis_aligned = true, z_axis_aligned = true;
+  double w[3] = {0, 0, 0};  // box width
+  double r = 0, h = 0;      // cylinder / sphere radius, cylinder height, ground height
+  std::vector<std::shared_ptr<HostSdf>> members;
+  std::shared_ptr<CloudData> cloud;
+
+  void touch() { version = g_sdf_version++; }
+  bool transformable() const { return kind == PM_SDF_BOX || kind == PM_SDF_CYLINDER || kind == PM_SDF_SPHERE; }
+  // Pose::update_alignment_flags_ and rot_.inverse() (primitive_sdf.hpp:30-68)
+  void update_pose() {
+    const double* R = rot;
+    double cof[9];
+    cof[0] = R[4] * R[8] - R[5] * R[7];
+    cof[1] = R[5] * R[6] - R[3] * R[8];
+    cof[2] = R[3] * R[7] - R[4] * R[6];
+    cof[3] = R[2] * R[7] - R[1] * R[8];
+    cof[4] = R[0] * R[8] - R[2] * R[6];
+    cof[5] = R[1] * R[6] - R[0] * R[7];
+    cof[6] = R[1] * R[5] - R[2] * R[4];
+    cof[7] = R[2] * R[3] - R[0] * R[5];
+    cof[8] = R[0] * R[4] - R[1] * R[3];
+    double det = R[0] * cof[0] + R[1] * cof[1] + R[2] * cof[2];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) rot_inv[3 * i + j] = cof[3 * j + i] / det;
+    double d2 = 0, n2 = 0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        double e = R[3 * i + j] - (i == j ? 1.0 : 0.0);
+        d2 += e * e;
+        n2 += R[3 * i + j] * R[3 * i + j];
+      }
+    axis_aligned = d2 <= 1e-12 * 1e-12 * std::min(n2, 3.0);  // Eigen isApprox with dummy_precision 1e-12
+    if (axis_aligned) {
+      z_axis_aligned = true;
+    } else {
+      const double tol = 1e-6;
+      z_axis_aligned = (std::abs(R[8] - 1.0) < tol) && (std::abs(R[2]) < tol) && (std::abs(R[5]) < tol) && (std::abs(R[6]) < tol) &&
+                       (std::abs(R[7]) < tol);
+    }
+  }
+  // update_aabb (primitive_sdf.hpp:250-255, 400-421, 500-521, 558-561)
+  void update_aabb() {
+    if (kind == PM_SDF_BOX || kind == PM_SDF_CYLINDER) {
+      double ex = kind == PM_SDF_BOX ? w[0] * 0.5 : r, ey = kind == PM_SDF_BOX ? w[1] * 0.5 : r,
+             ez = kind == PM_SDF_BOX ? w[2] * 0.5 : 0.5 * h;
+      const double sx[8] = {-ex, ex, -ex, ex, -ex, ex, -ex, ex};
+      const double sy[8] = {-ey, -ey, ey, ey, -ey, -ey, ey, ey};
+      const double sz[8] = {-ez, -ez, -ez, -ez, ez, ez, ez, ez};
+      for (int k = 0; k < 8; k++) {
+        double v[3];
+        for (int a = 0; a < 3; a++) v[a] = (rot[3 * a] * sx[k] + (rot[3 * a + 1] * sy[k] + rot[3 * a + 2] * sz[k])) + pos[a];
+        for (int a = 0; a < 3; a++) {
+          if (k == 0 || v[a] < lb[a]) lb[a] = v[a];
+          if (k == 0 || v[a] > ub[a]) ub[a] = v[a];
+        }
+      }
+    } else if (kind == PM_SDF_SPHERE) {
+      for (int a = 0; a < 3; a++) {
+        lb[a] = pos[a] - r;
+        ub[a] = pos[a] + r;
+      }
+    } else if (kind == PM_SDF_GROUND) {
+      const double inf = std::numeric_limits<double>::infinity();
+      lb[0] = lb[1] = -inf;
+      ub[0] = ub[1] = inf;
+      lb[2] = ub[2] = 0.0;
+    }
+  }
+  void translate(const double* t) {
+    if (kind == PM_SDF_UNION) {
+      for (auto& m : members) m->translate(t);
+      return;
+    }
+    if (kind == PM_SDF_GROUND) fail(PMGPU_ERR_RUNTIME, "GroundSDF does not support translation");
+    if (kind == PM_SDF_CLOUD) fail(PMGPU_ERR_RUNTIME, "TODO: Not implemented yet");
+    for (int a = 0; a < 3; a++) pos[a] += t[a];
+    update_aabb();
+    touch();
+  }
+  void rotate_z(double ang) {  // Pose::rotate_z (primitive_sdf.hpp:45-53)
+    if (kind == PM_SDF_UNION) {
+      for (auto& m : members) m->rotate_z(ang);
+      return;
+    }
+    if (kind == PM_SDF_GROUND) fail(PMGPU_ERR_RUNTIME, "GroundSDF does not support rotation");
+    if (kind == PM_SDF_CLOUD) fail(PMGPU_ERR_RUNTIME, "TODO: Not implemented yet");
+    double c = std::cos(ang), s = std::sin(ang);
+    const double rz[9] = {c, -s, 0, s, c, 0, 0, 0, 1};
+    double nr[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) nr[3 * i + j] = rz[3 * i] * rot[j] + (rz[3 * i + 1] * rot[3 + j] + rz[3 * i + 2] * rot[6 + j]);
+    std::memcpy(rot, nr, sizeof(rot));
+    update_pose();
+    update_aabb();
+    touch();
+  }
+  std::shared_ptr<HostSdf> clone() const {
+    if (kind == PM_SDF_CLOUD) fail(PMGPU_ERR_RUNTIME, "TODO: Not implemented yet");
+    auto c = std::make_shared<HostSdf>(*this);
+    if (kind == PM_SDF_UNION) {
+      c->members.clear();
+      for (auto& m : members) c->members.push_back(m->clone());
+    }
+    c->touch();
+    return c;
+  }
+  // PmPrim block of a leaf
+  PmPrim to_prim(int cloud_index) const {
+    PmPrim p;
+    std::memset(&p, 0, sizeof(p));
+    p.kind = kind;
+    p.axis_aligned = axis_aligned;
+    p.z_axis_aligned = z_axis_aligned;
+    p.cloud = cloud_index;
+    for (int a = 0; a < 3; a++) {
+      p.lb[a] = lb[a];
+      p.ub[a] = ub[a];
+      p.pos[a] = pos[a];
+    }
+    std::memcpy(p.rot, rot, sizeof(p.rot));
+    std::memcpy(p.rot_inv, rot_inv, sizeof(p.rot_inv));
+    switch (kind) {
+      case PM_SDF_BOX:
+        p.a = 0.5 * w[0];
+        p.b = 0.5 * w[1];
+        p.c = 0.5 * w[2];
+        break;
+      case PM_SDF_CYLINDER:
+        p.a = r;
+        p.b = r * r;
+        p.c = 0.5 * h;
+        break;
+      case PM_SDF_SPHERE:
+        p.a = r;
+        p.b = r * r;
+        break;
+      case PM_SDF_GROUND:
+        p.a = h;
+        break;
+      case PM_SDF_CLOUD:
+        p.a = cloud->radius;
+        break;
+    }
+    return p;
+  }
+};
+
+// set_all_sdfs_inner (primitive_sphere_collision.cpp:436-448)
+static void flatten(const std::shared_ptr<HostSdf>& s, std::vector<std::shared_ptr<HostSdf>>& out) {
+  if (s->kind == PM_SDF_UNION) {
+    for (auto& m : s->members) flatten(m, out);
+  } else {
+    out.push_back(s);
+  }
+}
+
+static void check_rotation(const double* rot) {
+  for (int i = 0; i < 9; i++)
+    if (!std::isfinite(rot[i])) throw std::invalid_argument("rotation matrix has non-finite entries");
+}
+
+// Device image of one SDF tree (for SDF-level evaluate / is_outside calls).
+struct SdfDeviceImage {
+  DevBuf prims, clouds;
+  int n_prims = 0;
+  std::vector<std::pair<const HostSdf*, uint64_t>> sig;
+};
+
+static void build_cloud(CloudData& cd) {
+  require_device();
+  int64_t n = (int64_t)(cd.pts.size() / 3);
+  DevBuf dpts;
+  dpts.ensure(std::max<size_t>(cd.pts.size() * 8, 8));
+  if (n > 0) cuda_check(cudaMemcpy(dpts.p, cd.pts.data(), cd.pts.size() * 8, cudaMemcpyHostToDevice), "cloud upload");
+  double lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = std::numeric_limits<double>::infinity();
+    hi[a] = -std::numeric_limits<double>::infinity();
+  }
+  for (int64_t i = 0; i < n; i++)
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::min(lo[a], cd.pts[3 * i + a]);
+      hi[a] = std::max(hi[a], cd.pts[3 * i + a]);
+    }
+  double cell = cd.cell > 0 ? cd.cell : 0.012;
+  double blk = cell * PM_GRID_B;
+  int nb[3];
+  for (;;) {
+    int64_t tot = 1;
+    for (int a = 0; a < 3; a++) {
+      double ext = n > 0 ? (hi[a] - lo[a]) : 0.0;
+      nb[a] = (int)std::floor(ext / blk) + 1;
+      tot *= nb[a];
+    }
+    if (tot * PM_GRID_CELLS_PER_BLOCK <= (int64_t)64 << 20) break;  // at most 64M fine cells
+    cell *= 1.25;
+    blk = cell * PM_GRID_B;
+  }
+  GridBuild& g = cd.g;
+  g.pts = dpts.as<double>();
+  g.n = n;
+  g.radius = cd.radius;
+  g.cell = cell;
+  g.dev.nbx = nb[0];
+  g.dev.nby = nb[1];
+  g.dev.nbz = nb[2];
+  for (int a = 0; a < 3; a++) g.dev.origin[a] = n > 0 ? lo[a] : 0.0;
+  g.dev.block = blk;
+  g.dev.radius = cd.radius;
+  for (int a = 0; a < 3; a++) {
+    g.dev.lb[a] = cd.lb[a];
+    g.dev.ub[a] = cd.ub[a];
+  }
+  cuda_check(grid_build(g, 0), "cloud grid build");
+  cd.built = true;
+  cd.cell = cell;
+  cd.d_grid.ensure(sizeof(PmGridDev));
+  cuda_check(cudaMemcpy(cd.d_grid.p, &g.dev, sizeof(PmGridDev), cudaMemcpyHostToDevice), "grid descriptor upload");
+}
+
+// ---------------------------------------------------------------------------- SphereCollisionCst
+struct HostGroup {
+  std::string link_name;
+  int link = 0;
+  std::vector<std::array<double, 3>> rel;
+  std::vector<double> radii;
+  double radius = 0;
+  std::array<double, 3> centre{0, 0, 0};
+  bool only_self = false;
+};
+
+// reorder_spheres_for_informative_collision_check (primitive_sphere_collision.cpp:53-96); the
+// unvisited set is walked in libstdc++ unordered_set order, i.e. descending index.
+static std::vector<size_t> farthest_order(const std::vector<std::array<double, 3>>& pos) {
+  size_t n = pos.size();
+  std::vector<size_t> visited;
+  if (n == 0) return visited;
+  std::vector<size_t> unvisited;
+  for (size_t i = n; i-- > 0;) unvisited.push_back(i);
+  visited.push_back(unvisited.front());
+  unvisited.erase(unvisited.begin());
+  auto nrm = [](const std::array<double, 3>& a, const std::array<double, 3>& b) {
+    double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+    return std::sqrt(d0 * d0 + (d1 * d1 + d2 * d2));
+  };
+  for (size_t it = 0; it + 1 < n; it++) {
+    double max_dist = 0.0;
+    size_t best = 0;
+    for (size_t k = 0; k < unvisited.size(); k++) {
+      double md = std::numeric_limits<double>::max();
+      for (size_t vv : visited) {
+        double d = nrm(pos[unvisited[k]], pos[vv]);
+        if (d < md) md = d;
+      }
+      if (md > max_dist) {
+        max_dist = md;
+        best = k;
+      }
+    }
+    visited.push_back(unvisited[best]);
+    unvisited.erase(unvisited.begin() + best);
+  }
+  return visited;
+}
+
+struct HostCst {
+  std::shared_ptr<HostModel> kin;
+  std::vector<int> ids;
+  int base_type = PM_BASE_FIXED;
+  std::vector<HostGroup> groups;
+  std::vector<std::pair<int, int>> pairs;
+  std::shared_ptr<HostSdf> fixed_sdf, sdf;
+  // device tables and their signature
+  DevBuf d_tables;
+  std::vector<std::pair<const HostSdf*, uint64_t>> sig;
+  uint64_t sig_model_version = 0;
+  std::vector<std::shared_ptr<HostSdf>> flat;
+  std::vector<int> slot_of_link;
+  std::vector<PmSlot> ctrl_recs;  // per control joint (child link, REV/PRIS) for state updates
+  DevBuf d_ctrl_recs;
+  // workspaces for host-memory calls
+  DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
+  std::vector<int16_t> seq_host;
+
+  int q_dim() const { return (int)ids.size() + (base_type == PM_BASE_FLOATING) * 6 + (base_type == PM_BASE_PLANAR) * 3; }
+  int n_spheres() const {
+    int n = 0;
+    for (auto& g : groups) n += (int)g.radii.size();
+    return n;
+  }
+  int cst_dim() {
+    std::vector<std::shared_ptr<HostSdf>> f;
+    if (fixed_sdf) flatten(fixed_sdf, f);
+    if (sdf) flatten(sdf, f);
+    return (f.empty() ? 0 : 1) + (pairs.empty() ? 0 : 1);
+  }
+
+  const PmTablesHdr* tables() {
+    kin->ensure_device();
+    std::vector<std::shared_ptr<HostSdf>> f;
+    if (fixed_sdf) flatten(fixed_sdf, f);
+    if (sdf) flatten(sdf, f);
+    std::vector<std::pair<const HostSdf*, uint64_t>> s;
+    for (auto& x : f) s.push_back({x.get(), x->version});
+    if (d_tables.p && s == sig && sig_model_version == kin->version) return d_tables.as<PmTablesHdr>();
+    flat = f;
+    build_tables();
+    sig = s;
+    sig_model_version = kin->version;
+    return d_tables.as<PmTablesHdr>();
+  }
+
+  void build_tables() {
+    HostModel& m = *kin;
+    const int nl = m.n_link();
+    // links the constraint touches: sphere links and all their ancestors (+ root)
+    std::vector<char> need(nl, 0);
+    need[m.root] = 1;
+    for (auto& g : groups)
+      for (int l = g.link; l >= 0; l = m.parent[l]) need[l] = 1;
+    std::vector<int> links;
+    for (int l = 0; l < nl; l++)
+      if (need[l]) links.push_back(l);  // DFS numbering puts parents before children
+    if ((int)links.size() > PM_MAX_SLOTS)
+      fail(PMGPU_ERR_INVALID, "constraint touches " + std::to_string(links.size()) + " links; the device limit is " +
+                                  std::to_string(PM_MAX_SLOTS));
+    if ((int)ids.size() > PM_MAX_CTRL) fail(PMGPU_ERR_INVALID, "more than 64 control joints");
+    slot_of_link.assign(nl, -1);
+    for (size_t i = 0; i < links.size(); i++) slot_of_link[links[i]] = (int)i;
+    // which control column drives each link (the last occurrence wins, as in set_joint_angles)
+    std::vector<int> ctrl_col(nl, -1);
+    for (size_t i = 0; i < ids.size(); i++) ctrl_col[m.joints[ids[i]].child] = (int)i;
+    // subtree membership for the relevance table (kinematics.cpp:340-363)
+    auto in_subtree = [&](int link, int top) {
+      for (int l = link; l >= 0; l = m.parent[l])
+        if (l == top) return true;
+      return false;
+    };
+    std::vector<PmSlot> slots(links.size());
+    for (size_t i = 0; i < links.size(); i++) {
+      PmSlot& s = slots[i];
+      std::memset(&s, 0, sizeof(s));
+      int l = links[i];
+      s.link = l;
+      s.parent = m.parent[l] < 0 ? -1 : slot_of_link[m.parent[l]];
+      s.mode = PM_FK_STATE;
+      s.qcol = -1;
+      if (ctrl_col[l] >= 0) {
+        const HostJoint& j = m.joints[ids[ctrl_col[l]]];
+        s.mode = j.type == UJ_PRISMATIC ? PM_FK_PRIS : PM_FK_REV;
+        s.qcol = ctrl_col[l];
+        s.origin_identity = j.qid;
+        std::memcpy(s.axis, j.axis, sizeof(s.axis));
+        std::memcpy(s.oq, j.quat, sizeof(s.oq));
+        std::memcpy(s.ot, j.pos, sizeof(s.ot));
+      }
+      uint64_t rel = 0;
+      for (size_t c = 0; c < ids.size(); c++)
+        if (in_subtree(l, m.joints[ids[c]].child)) rel |= (1ull << c);
+      s.relevant = rel;
+    }
+    std::vector<PmJoint> jrec(ids.size());
+    for (size_t c = 0; c < ids.size(); c++) {
+      const HostJoint& j = m.joints[ids[c]];
+      jrec[c].slot = slot_of_link[j.child];
+      jrec[c].prismatic = j.type == UJ_PRISMATIC;
+      std::memcpy(jrec[c].axis, j.axis, sizeof(jrec[c].axis));
+    }
+    std::vector<PmGroup> grec(groups.size());
+    std::vector<double> sx, sy, sz, sr;
+    std::vector<int32_t> sgroup;
+    for (size_t g = 0; g < groups.size(); g++) {
+      const HostGroup& G = groups[g];
+      grec[g].slot = slot_of_link[G.link];
+      grec[g].begin = (int)sx.size();
+      grec[g].count = (int)G.radii.size();
+      grec[g].only_self = G.only_self;
+      for (int a = 0; a < 3; a++) grec[g].rel[a] = G.centre[a];
+      grec[g].radius = G.radius;
+      for (size_t k = 0; k < G.radii.size(); k++) {
+        sx.push_back(G.rel[k][0]);
+        sy.push_back(G.rel[k][1]);
+        sz.push_back(G.rel[k][2]);
+        sr.push_back(G.radii[k]);
+        sgroup.push_back((int)g);
+      }
+    }
+    std::vector<int32_t> prs;
+    for (auto& p : pairs) {
+      prs.push_back(p.first);
+      prs.push_back(p.second);
+    }
+    std::vector<PmPrim> prims;
+    std::vector<PmGridDev> clouds;
+    for (auto& x : flat) {
+      int ci = -1;
+      if (x->kind == PM_SDF_CLOUD) {
+        if (!x->cloud->built) build_cloud(*x->cloud);
+        ci = (int)clouds.size();
+        clouds.push_back(x->cloud->g.dev);
+      }
+      prims.push_back(x->to_prim(ci));
+    }
+    // pack
+    PmTablesHdr h;
+    std::memset(&h, 0, sizeof(h));
+    h.n_slots = (int)slots.size();
+    h.n_ctrl = (int)ids.size();
+    h.n_groups = (int)grec.size();
+    h.n_spheres = (int)sr.size();
+    h.n_pairs = (int)pairs.size();
+    h.n_prims = (int)prims.size();
+    h.q_dim = q_dim();
+    h.base_type = base_type;
+    h.root_slot = slot_of_link[m.root];
+    h.n_clouds = (int)clouds.size();
+    std::vector<char> buf;
+    auto align = [&]() {
+      while (buf.size() % 16) buf.push_back(0);
+    };
+    auto put = [&](const void* p, size_t bytes) -> int64_t {
+      align();
+      int64_t off = (int64_t)buf.size();
+      buf.insert(buf.end(), (const char*)p, (const char*)p + bytes);
+      return off;
+    };
+    buf.resize(sizeof(PmTablesHdr));
+    h.off_slots = put(slots.data(), slots.size() * sizeof(PmSlot));
+    h.off_joints = put(jrec.data(), jrec.size() * sizeof(PmJoint));
+    h.off_groups = put(grec.data(), grec.size() * sizeof(PmGroup));
+    h.off_sx = put(sx.data(), sx.size() * 8);
+    h.off_sy = put(sy.data(), sy.size() * 8);
+    h.off_sz = put(sz.data(), sz.size() * 8);
+    h.off_sr = put(sr.data(), sr.size() * 8);
+    h.off_sgroup = put(sgroup.data(), sgroup.size() * 4);
+    h.off_pairs = put(prs.data(), prs.size() * 4);
+    h.off_prims = put(prims.data(), prims.size() * sizeof(PmPrim));
+    h.off_clouds = put(clouds.data(), clouds.size() * sizeof(PmGridDev));
+    align();
+    h.total_bytes = (int64_t)buf.size();
+    std::memcpy(buf.data(), &h, sizeof(h));
+    d_tables.release();
+    d_tables.ensure(buf.size());
+    cuda_check(cudaMemcpy(d_tables.p, buf.data(), buf.size(), cudaMemcpyHostToDevice), "tables upload");
+    // control joint records for update_kintree
+    ctrl_recs.resize(ids.size());
+    for (size_t c = 0; c < ids.size(); c++) {
+      const HostJoint& j = m.joints[ids[c]];
+      PmSlot& s = ctrl_recs[c];
+      std::memset(&s, 0, sizeof(s));
+      s.link = j.child;
+      s.mode = j.type == UJ_PRISMATIC ? PM_FK_PRIS : PM_FK_REV;
+      s.origin_identity = j.qid;
+      std::memcpy(s.axis, j.axis, sizeof(s.axis));
+      std::memcpy(s.oq, j.quat, sizeof(s.oq));
+      std::memcpy(s.ot, j.pos, sizeof(s.ot));
+    }
+    d_ctrl_recs.release();
+    d_ctrl_recs.ensure(std::max<size_t>(ctrl_recs.size(), 1) * sizeof(PmSlot));
+    if (!ctrl_recs.empty())
+      cuda_check(cudaMemcpy(d_ctrl_recs.p, ctrl_recs.data(), ctrl_recs.size() * sizeof(PmSlot), cudaMemcpyHostToDevice),
+                 "control records upload");
+  }
+
+  const int16_t* seq_table() {
+    if (!w_seq.p) {
+      // find_farthest_sequence_fast (ompl/generate_sequence.py:11-63), 128 x 128
+      seq_host.assign(128 * 128, 0);
+      for (int n = 1; n <= 128; n++) {
+        std::vector<int> res(n, 0);
+        std::vector<char> used(n, 0);
+        used[0] = 1;
+        for (int i = 1; i < n; i++) {
+          int best_md = -1, best = -1;
+          for (int num = 0; num < n; num++) {
+            if (used[num]) continue;
+            int md = std::numeric_limits<int>::max();
+            for (int j = 0; j < i; j++) md = std::min(md, std::abs(num - res[j]));
+            if (md > best_md || (md == best_md && num > best)) {
+              best_md = md;
+              best = num;
+            }
+          }
+          res[i] = best;
+          used[best] = 1;
+        }
+        for (int j = 0; j < n; j++) seq_host[(n - 1) * 128 + j] = (int16_t)res[j];
+      }
+      w_seq.ensure(seq_host.size() * 2);
+      cuda_check(cudaMemcpy(w_seq.p, seq_host.data(), seq_host.size() * 2, cudaMemcpyHostToDevice), "sequence upload");
+    }
+    return w_seq.as<int16_t>();
+  }
+};
+
+}  // namespace pmg
+
+// ============================================================================ C ABI
+using namespace pmg;
+
+struct pmgpu_model {
+  std::shared_ptr<HostModel> m;
+};
+struct pmgpu_sdf {
+  std::shared_ptr<HostSdf> s;
+  SdfDeviceImage img;
+};
+struct pmgpu_cst {
+  HostCst c;
+};
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+void check_mem(int mem) {
+  if (mem != PMGPU_MEM_HOST && mem != PMGPU_MEM_DEVICE) throw std::invalid_argument("mem must be PMGPU_MEM_HOST or PMGPU_MEM_DEVICE");
+}
+void check_ptr(const void* p, const char* what) {
+  if (!p) throw std::invalid_argument(std::string(what) + " is NULL");
+}
+
+// Device image of an SDF tree for SDF-level calls
+const PmPrim* sdf_image(pmgpu_sdf* h, int* n_prims, const PmGridDev** clouds) {
+  std::vector<std::shared_ptr<HostSdf>> f;
+  flatten(h->s, f);
+  std::vector<std::pair<const HostSdf*, uint64_t>> sig;
+  for (auto& x : f) sig.push_back({x.get(), x->version});
+  if (!h->img.prims.p || sig != h->img.sig) {
+    require_device();
+    std::vector<PmPrim> prims;
+    std::vector<PmGridDev> cl;
+    for (auto& x : f) {
+      int ci = -1;
+      if (x->kind == PM_SDF_CLOUD) {
+        if (!x->cloud->built) build_cloud(*x->cloud);
+        ci = (int)cl.size();
+        cl.push_back(x->cloud->g.dev);
+      }
+      prims.push_back(x->to_prim(ci));
+    }
+    h->img.prims.release();
+    h->img.prims.ensure(std::max<size_t>(prims.size(), 1) * sizeof(PmPrim));
+    if (!prims.empty()) cuda_check(cudaMemcpy(h->img.prims.p, prims.data(), prims.size() * sizeof(PmPrim), cudaMemcpyHostToDevice), "sdf upload");
+    h->img.clouds.release();
+    h->img.clouds.ensure(std::max<size_t>(cl.size(), 1) * sizeof(PmGridDev));
+    if (!cl.empty()) cuda_check(cudaMemcpy(h->img.clouds.p, cl.data(), cl.size() * sizeof(PmGridDev), cudaMemcpyHostToDevice), "sdf upload");
+    h->img.n_prims = (int)prims.size();
+    h->img.sig = sig;
+  }
+  *n_prims = h->img.n_prims;
+  *clouds = h->img.clouds.as<PmGridDev>();
+  return h->img.prims.as<PmPrim>();
+}
+
+// Host-memory staging: copies `bytes` from host to a workspace buffer, returns device ptr
+template <class T>
+T* stage_in(DevBuf& buf, const T* host, size_t count, cudaStream_t s) {
+  T* d = reinterpret_cast<T*>(buf.ensure(std::max<size_t>(count * sizeof(T), 16)));
+  if (count) cuda_check(cudaMemcpyAsync(d, host, count * sizeof(T), cudaMemcpyHostToDevice, s), "H2D copy");
+  return d;
+}
+template <class T>
+void stage_out(T* host, const T* dev, size_t count, cudaStream_t s) {
+  if (count) cuda_check(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, s), "D2H copy");
+}
+
+void check_joint_ids(const HostModel& m, const int64_t* ids, int n) {
+  for (int i = 0; i < n; i++)
+    if (ids[i] < 0 || ids[i] >= (int64_t)m.joints.size()) throw std::invalid_argument("joint id out of range");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pmgpu_last_error(void) { return g_last_error.c_str(); }
+int pmgpu_version(void) { return 100; }
+int pmgpu_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+// ---------------------------------------------------------------- model
+int pmgpu_model_create(const char* urdf_xml, pmgpu_model** out) {
+  return guarded([&] {
+    check_ptr(urdf_xml, "urdf_xml");
+    check_ptr(out, "out");
+    auto* h = new pmgpu_model();
+    try {
+      h->m = build_model(urdf_xml);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+void pmgpu_model_destroy(pmgpu_model* m) { delete m; }
+int pmgpu_model_counts(const pmgpu_model* m, int* n_links, int* n_joints, int* root_link) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    if (n_links) *n_links = m->m->n_link();
+    if (n_joints) *n_joints = (int)m->m->joints.size();
+    if (root_link) *root_link = m->m->root;
+  });
+}
+int pmgpu_model_get_joint_ids(const pmgpu_model* m, const char* const* names, int n, int64_t* ids_out) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    for (int i = 0; i < n; i++) {
+      auto it = m->m->joint_id.find(names[i]);
+      if (it == m->m->joint_id.end()) throw std::invalid_argument(std::string("no joint named ") + names[i]);
+      ids_out[i] = it->second;
+    }
+  });
+}
+int pmgpu_model_get_link_ids(const pmgpu_model* m, const char* const* names, int n, int64_t* ids_out) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    for (int i = 0; i < n; i++) {
+      auto it = m->m->link_id.find(names[i]);
+      if (it == m->m->link_id.end()) throw std::invalid_argument(std::string("no link named ") + names[i]);
+      ids_out[i] = it->second;
+    }
+  });
+}
+int pmgpu_model_get_joint_position_limits(const pmgpu_model* m, const int64_t* ids, int n, double* lower, double* upper) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    check_joint_ids(*m->m, ids, n);
+    for (int i = 0; i < n; i++) {
+      lower[i] = m->m->joints[ids[i]].lower;
+      upper[i] = m->m->joints[ids[i]].upper;
+    }
+  });
+}
+int pmgpu_model_link_name(const pmgpu_model* m, int64_t id, char* buf, int cap) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    if (id < 0 || id >= m->m->n_link()) throw std::invalid_argument("link id out of range");
+    std::snprintf(buf, (size_t)cap, "%s", m->m->link_name[id].c_str());
+  });
+}
+int pmgpu_model_joint_name(const pmgpu_model* m, int64_t id, char* buf, int cap) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    if (id < 0 || id >= (int64_t)m->m->joints.size()) throw std::invalid_argument("joint id out of range");
+    std::snprintf(buf, (size_t)cap, "%s", m->m->joints[id].name.c_str());
+  });
+}
+int pmgpu_model_structure(const pmgpu_model* m, int32_t* link_parent, double* link_tf7, int32_t* link_tf_qid, int32_t* joint_child,
+                          int32_t* joint_type, double* joint_axis3, int32_t* joint_origin_qid) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    const HostModel& M = *m->m;
+    for (int l = 0; l < M.n_link(); l++) {
+      if (link_parent) link_parent[l] = M.parent[l];
+      const double* r = M.state_init.data() + (size_t)PM_STATE_LINK_ROW(l) * PM_STATE_STRIDE;
+      if (link_tf7) {
+        double v[7] = {r[4], r[5], r[6], r[0], r[1], r[2], r[3]};
+        std::memcpy(link_tf7 + 7 * l, v, sizeof(v));
+      }
+      if (link_tf_qid) link_tf_qid[l] = r[7] != 0.0;
+    }
+    for (size_t j = 0; j < M.joints.size(); j++) {
+      if (joint_child) joint_child[j] = M.joints[j].child;
+      if (joint_type) joint_type[j] = M.joints[j].type;
+      if (joint_axis3) std::memcpy(joint_axis3 + 3 * j, M.joints[j].axis, 24);
+      if (joint_origin_qid) joint_origin_qid[j] = M.joints[j].qid;
+    }
+  });
+}
+int pmgpu_model_set_joint_positions(pmgpu_model* m, const int64_t* ids, int n, const double* q, int accurate) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    HostModel& M = *m->m;
+    check_joint_ids(M, ids, n);
+    M.ensure_device();
+    std::vector<PmSlot> recs(n);
+    for (int i = 0; i < n; i++) {
+      const HostJoint& j = M.joints[ids[i]];
+      PmSlot& s = recs[i];
+      std::memset(&s, 0, sizeof(s));
+      s.link = j.child;
+      s.mode = j.type == UJ_PRISMATIC ? PM_FK_PRIS : PM_FK_REV;
+      s.origin_identity = j.qid;
+      std::memcpy(s.axis, j.axis, 24);
+      std::memcpy(s.oq, j.quat, 32);
+      std::memcpy(s.ot, j.pos, 24);
+      M.angles[ids[i]] = q[i];
+    }
+    if (n == 0) return;
+    size_t rb = recs.size() * sizeof(PmSlot);
+    char* d = (char*)M.d_scratch.ensure(rb + (size_t)n * 8 + 64);
+    cuda_check(cudaMemcpy(d, recs.data(), rb, cudaMemcpyHostToDevice), "H2D");
+    double* dq = (double*)(d + ((rb + 15) / 16) * 16);
+    cuda_check(cudaMemcpy(dq, q, (size_t)n * 8, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(launch_set_joints(M.d_state.as<double>(), (const PmSlot*)d, dq, n, accurate, 0), "set joints");
+    cuda_check(cudaDeviceSynchronize(), "set joints");
+  });
+}
+int pmgpu_model_get_joint_positions(const pmgpu_model* m, const int64_t* ids, int n, double* q) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    check_joint_ids(*m->m, ids, n);
+    for (int i = 0; i < n; i++) q[i] = m->m->angles[ids[i]];
+  });
+}
+int pmgpu_model_set_base_pose(pmgpu_model* m, const double* pose7) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    HostModel& M = *m->m;
+    std::memcpy(M.base7, pose7, sizeof(M.base7));
+    const double q[4] = {pose7[3], pose7[4], pose7[5], pose7[6]}, t[3] = {pose7[0], pose7[1], pose7[2]};
+    set_row(M.state_init, PM_STATE_BASE_ROW, q, t, false);
+    if (M.dev_ready) {
+      double row[PM_STATE_STRIDE] = {q[0], q[1], q[2], q[3], t[0], t[1], t[2], 0.0};
+      cuda_check(cudaMemcpy(M.d_state.p, row, sizeof(row), cudaMemcpyHostToDevice), "base pose upload");
+    }
+  });
+}
+int pmgpu_model_get_base_pose(const pmgpu_model* m, double* pose7) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    const HostModel& M = *m->m;
+    if (M.dev_ready) {
+      double row[PM_STATE_STRIDE];
+      cuda_check(cudaMemcpy(row, M.d_state.p, sizeof(row), cudaMemcpyDeviceToHost), "base pose readback");
+      double v[7] = {row[4], row[5], row[6], row[0], row[1], row[2], row[3]};
+      std::memcpy(pose7, v, sizeof(v));
+    } else {
+      std::memcpy(pose7, M.base7, sizeof(M.base7));
+    }
+  });
+}
+int pmgpu_model_link_poses(pmgpu_model* m, const int64_t* link_ids, int n, double* out7) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    HostModel& M = *m->m;
+    for (int i = 0; i < n; i++)
+      if (link_ids[i] < 0 || link_ids[i] >= M.n_link()) throw std::invalid_argument("link id out of range");
+    M.ensure_device();
+    if (n == 0) return;
+    std::vector<int32_t> l32(link_ids, link_ids + n);
+    char* d = (char*)M.d_scratch.ensure((size_t)n * 4 + (size_t)n * 56 + 64);
+    double* dout = (double*)(d + (((size_t)n * 4 + 15) / 16) * 16);
+    cuda_check(cudaMemcpy(d, l32.data(), (size_t)n * 4, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(launch_link_poses(M.d_state.as<double>(), M.d_parents.as<int32_t>(), (const int32_t*)d, n, dout, 0), "link poses");
+    cuda_check(cudaMemcpy(out7, dout, (size_t)n * 56, cudaMemcpyDeviceToHost), "D2H");
+  });
+}
+int pmgpu_model_add_new_link(pmgpu_model* m, const char* name, const char* parent, const double* xyz, const double* rpy,
+                             int consider_rotation, int64_t* id_out) {
+  return guarded([&] {
+    check_ptr(m, "model");
+    HostModel& M = *m->m;
+    auto pit = M.link_id.find(parent);
+    if (pit == M.link_id.end()) throw std::invalid_argument(std::string("no link named ") + parent);
+    if (M.link_id.count(name)) fail(PMGPU_ERR_RUNTIME, std::string("link name : ") + name + " already exists");
+    int id = M.n_link();
+    M.link_id[name] = id;
+    M.link_name.push_back(name);
+    M.parent.push_back(pit->second);
+    M.children.push_back({});
+    M.children[pit->second].push_back(id);
+    M.consider_rotation.push_back(consider_rotation ? 1 : 0);
+    M.link_parent_joint.push_back(-1);
+    double q[4];
+    quat_from_rpy(rpy[0], rpy[1], rpy[2], q);
+    const double qi[4] = {0, 0, 0, 1};
+    M.state_init.resize((size_t)(id + 2) * PM_STATE_STRIDE, 0.0);
+    // consider_rotation=false keeps only the translation (algorithm.cpp:164-178)
+    if (consider_rotation)
+      set_row(M.state_init, PM_STATE_LINK_ROW(id), q, xyz, false);
+    else
+      set_row(M.state_init, PM_STATE_LINK_ROW(id), qi, xyz, true);
+    M.version++;
+    if (M.dev_ready) {
+      M.dev_ready = true;  // ensure_device() re-uploads with the appended row
+      M.ensure_device();
+      const double* r = M.state_init.data() + (size_t)PM_STATE_LINK_ROW(id) * PM_STATE_STRIDE;
+      cuda_check(cudaMemcpy(M.d_state.as<double>() + (size_t)PM_STATE_LINK_ROW(id) * PM_STATE_STRIDE, r, PM_STATE_STRIDE * 8,
+                            cudaMemcpyHostToDevice),
+                 "new link upload");
+    }
+    if (id_out) *id_out = id;
+  });
+}
+
+// ---------------------------------------------------------------- SDFs
+int pmgpu_pose_flags(const double* rot9, int* axis_aligned, int* z_axis_aligned, double* rot_inv9) {
+  return guarded([&] {
+    check_ptr(rot9, "rotation");
+    check_rotation(rot9);
+    HostSdf tmp;
+    std::memcpy(tmp.rot, rot9, 72);
+    tmp.update_pose();
+    if (axis_aligned) *axis_aligned = tmp.axis_aligned;
+    if (z_axis_aligned) *z_axis_aligned = tmp.z_axis_aligned;
+    if (rot_inv9) std::memcpy(rot_inv9, tmp.rot_inv, 72);
+  });
+}
+static pmgpu_sdf* wrap(std::shared_ptr<HostSdf> s) {
+  auto* h = new pmgpu_sdf();
+  h->s = std::move(s);
+  return h;
+}
+int pmgpu_sdf_box_create(const double* width3, const double* pos3, const double* rot9, pmgpu_sdf** out) {
+  return guarded([&] {
+    check_rotation(rot9);
+    auto s = std::make_shared<HostSdf>();
+    s->kind = PM_SDF_BOX;
+    std::memcpy(s->w, width3, 24);
+    std::memcpy(s->pos, pos3, 24);
+    std::memcpy(s->rot, rot9, 72);
+    s->update_pose();
+    s->update_aabb();
+    s->touch();
+    *out = wrap(s);
+  });
+}
+int pmgpu_sdf_cylinder_create(double radius, double height, const double* pos3, const double* rot9, pmgpu_sdf** out) {
+  return guarded([&] {
+    check_rotation(rot9);
+    auto s = std::make_shared<HostSdf>();
+    s->kind = PM_SDF_CYLINDER;
+    s->r = radius;
+    s->h = height;
+    std::memcpy(s->pos, pos3, 24);
+    std::memcpy(s->rot, rot9, 72);
+    s->update_pose();
+    s->update_aabb();
+    s->touch();
+    *out = wrap(s);
+  });
+}
+int pmgpu_sdf_sphere_create(double radius, const double* pos3, const double* rot9, pmgpu_sdf** out) {
+  return guarded([&] {
+    check_rotation(rot9);
+    auto s = std::make_shared<HostSdf>();
+    s->kind = PM_SDF_SPHERE;
+    s->r = radius;
+    std::memcpy(s->pos, pos3, 24);
+    std::memcpy(s->rot, rot9, 72);
+    s->update_pose();
+    s->update_aabb();
+    s->touch();
+    *out = wrap(s);
+  });
+}
+int pmgpu_sdf_ground_create(double height, pmgpu_sdf** out) {
+  return guarded([&] {
+    auto s = std::make_shared<HostSdf>();
+    s->kind = PM_SDF_GROUND;
+    s->h = height;
+    s->update_aabb();
+    s->touch();
+    *out = wrap(s);
+  });
+}
+int pmgpu_sdf_cloud_create(const double* points, int64_t n, double radius, double cell_size, pmgpu_sdf** out) {
+  return guarded([&] {
+    if (n < 0) throw std::invalid_argument("negative point count");
+    if (n > 0) check_ptr(points, "points");
+    if (n > (int64_t)1 << 30) throw std::invalid_argument("cloud too large");
+    auto s = std::make_shared<HostSdf>();
+    s->kind = PM_SDF_CLOUD;
+    auto cd = std::make_shared<CloudData>();
+    cd->pts.assign(points, points + 3 * n);
+    for (int64_t i = 0; i < 3 * n; i++)
+      if (!std::isfinite(cd->pts[i])) throw std::invalid_argument("cloud point with a non-finite coordinate");
+    cd->radius = radius;
+    cd->cell = cell_size;
+    // CloudSDF ctor (primitive_sdf.hpp:571-583)
+    for (int a = 0; a < 3; a++) {
+      cd->lb[a] = std::numeric_limits<double>::infinity();
+      cd->ub[a] = -std::numeric_limits<double>::infinity();
+    }
+    for (int64_t i = 0; i < n; i++)
+      for (int a = 0; a < 3; a++) {
+        cd->lb[a] = std::min(cd->lb[a], cd->pts[3 * i + a]);
+        cd->ub[a] = std::max(cd->ub[a], cd->pts[3 * i + a]);
+      }
+    for (int a = 0; a < 3; a++) {
+      cd->lb[a] -= radius;
+      cd->ub[a] += radius;
+      s->lb[a] = cd->lb[a];
+      s->ub[a] = cd->ub[a];
+    }
+    s->cloud = cd;
+    s->touch();
+    *out = wrap(s);
+  });
+}
+int pmgpu_sdf_union_create(pmgpu_sdf* const* members, int n, pmgpu_sdf** out) {
+  return guarded([&] {
+    auto s = std::make_shared<HostSdf>();
+    s->kind = PM_SDF_UNION;
+    for (int i = 0; i < n; i++) {
+      check_ptr(members[i], "member");
+      s->members.push_back(members[i]->s);
+    }
+    s->touch();
+    *out = wrap(s);
+  });
+}
+int pmgpu_sdf_union_add(pmgpu_sdf* u, pmgpu_sdf* member, int clone) {
+  return guarded([&] {
+    check_ptr(u, "union");
+    check_ptr(member, "member");
+    if (u->s->kind != PM_SDF_UNION) throw std::invalid_argument("not a UnionSDF");
+    u->s->members.push_back(clone ? member->s->clone() : member->s);
+    u->s->touch();
+  });
+}
+int pmgpu_sdf_clone(const pmgpu_sdf* s, pmgpu_sdf** out) {
+  return guarded([&] {
+    check_ptr(s, "sdf");
+    *out = wrap(s->s->clone());
+  });
+}
+void pmgpu_sdf_destroy(pmgpu_sdf* s) { delete s; }
+int pmgpu_sdf_translate(pmgpu_sdf* s, const double* t3) {
+  return guarded([&] {
+    check_ptr(s, "sdf");
+    s->s->translate(t3);
+  });
+}
+int pmgpu_sdf_rotate_z(pmgpu_sdf* s, double angle) {
+  return guarded([&] {
+    check_ptr(s, "sdf");
+    s->s->rotate_z(angle);
+  });
+}
+int pmgpu_sdf_info(const pmgpu_sdf* s, int* kind, double* lb3, double* ub3, int* axis_aligned, int* z_axis_aligned, double* pos3,
+                   double* rot9) {
+  return guarded([&] {
+    check_ptr(s, "sdf");
+    const HostSdf& x = *s->s;
+    if (kind) *kind = x.kind;
+    if (lb3) std::memcpy(lb3, x.lb, 24);
+    if (ub3) std::memcpy(ub3, x.ub, 24);
+    if (axis_aligned) *axis_aligned = x.axis_aligned;
+    if (z_axis_aligned) *z_axis_aligned = x.z_axis_aligned;
+    if (pos3) std::memcpy(pos3, x.pos, 24);
+    if (rot9) std::memcpy(rot9, x.rot, 72);
+  });
+}
+int pmgpu_sdf_evaluate(pmgpu_sdf* s, const double* points, int64_t n, double* out, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(s, "sdf");
+    check_mem(mem);
+    if (n < 0) throw std::invalid_argument("negative count");
+    int np;
+    const PmGridDev* cl;
+    const PmPrim* pr = sdf_image(s, &np, &cl);
+    cudaStream_t st = as_stream(stream);
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_sdf_points(pr, np, cl, s->s->kind == PM_SDF_UNION, points, nullptr, n, out, nullptr, st), "sdf evaluate");
+      return;
+    }
+    DevBuf a, b;
+    const double* dp = stage_in(a, points, (size_t)n * 3, st);
+    double* dout = (double*)b.ensure(std::max<size_t>((size_t)n * 8, 16));
+    cuda_check(launch_sdf_points(pr, np, cl, s->s->kind == PM_SDF_UNION, dp, nullptr, n, dout, nullptr, st), "sdf evaluate");
+    stage_out(out, dout, (size_t)n, st);
+    cuda_check(cudaStreamSynchronize(st), "sdf evaluate");
+  });
+}
+int pmgpu_sdf_is_outside(pmgpu_sdf* s, const double* points, const double* radii, int64_t n, uint8_t* out, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(s, "sdf");
+    check_mem(mem);
+    if (n < 0) throw std::invalid_argument("negative count");
+    int np;
+    const PmGridDev* cl;
+    const PmPrim* pr = sdf_image(s, &np, &cl);
+    cudaStream_t st = as_stream(stream);
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_sdf_points(pr, np, cl, 1, points, radii, n, nullptr, out, st), "sdf is_outside");
+      return;
+    }
+    DevBuf a, b, c;
+    const double* dp = stage_in(a, points, (size_t)n * 3, st);
+    const double* dr = stage_in(b, radii, (size_t)n, st);
+    uint8_t* dout = (uint8_t*)c.ensure(std::max<size_t>((size_t)n, 16));
+    cuda_check(launch_sdf_points(pr, np, cl, 1, dp, dr, n, nullptr, dout, st), "sdf is_outside");
+    stage_out(out, dout, (size_t)n, st);
+    cuda_check(cudaStreamSynchronize(st), "sdf is_outside");
+  });
+}
+int pmgpu_cloud_nearest(pmgpu_sdf* cloud, const double* points, int64_t n, double* sqdist, double* nearest3, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(cloud, "cloud");
+    check_mem(mem);
+    if (cloud->s->kind != PM_SDF_CLOUD) throw std::invalid_argument("not a CloudSDF");
+    int np;
+    const PmGridDev* cl;
+    sdf_image(cloud, &np, &cl);
+    cudaStream_t st = as_stream(stream);
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_cloud_nearest(cl, points, n, sqdist, nearest3, st), "cloud nearest");
+      return;
+    }
+    DevBuf a, b, c;
+    const double* dp = stage_in(a, points, (size_t)n * 3, st);
+    double* dsq = sqdist ? (double*)b.ensure(std::max<size_t>((size_t)n * 8, 16)) : nullptr;
+    double* dnr = nearest3 ? (double*)c.ensure(std::max<size_t>((size_t)n * 24, 16)) : nullptr;
+    cuda_check(launch_cloud_nearest(cl, dp, n, dsq, dnr, st), "cloud nearest");
+    if (sqdist) stage_out(sqdist, dsq, (size_t)n, st);
+    if (nearest3) stage_out(nearest3, dnr, (size_t)n * 3, st);
+    cuda_check(cudaStreamSynchronize(st), "cloud nearest");
+  });
+}
+
+// ---------------------------------------------------------------- SphereCollisionCst
+int pmgpu_cst_create(pmgpu_model* kin, const char* const* control_joints, int n_joints, int base_type, int n_specs,
+                     const char* const* spec_links, const int32_t* counts, const double* rel_xyz, const double* radii,
+                     const uint8_t* only_self, int n_pairs, const char* const* pair_a, const char* const* pair_b, pmgpu_sdf* fixed_sdf,
+                     int reorder_spheres, pmgpu_cst** out) {
+  return guarded([&] {
+    check_ptr(kin, "kin");
+    if (base_type < 0 || base_type > 2) throw std::invalid_argument("unknown base type");
+    auto* h = new pmgpu_cst();
+    try {
+      HostCst& c = h->c;
+      c.kin = kin->m;
+      HostModel& M = *c.kin;
+      for (int i = 0; i < n_joints; i++) {  // ConstraintBase ctor -> get_joint_ids (primitive.hpp:30-36)
+        auto it = M.joint_id.find(control_joints[i]);
+        if (it == M.joint_id.end()) throw std::invalid_argument(std::string("no joint named ") + control_joints[i]);
+        c.ids.push_back(it->second);
+      }
+      c.base_type = base_type;
+      size_t off = 0;
+      for (int s = 0; s < n_specs; s++) {  // primitive_sphere_collision.cpp:127-160
+        HostGroup g;
+        g.link_name = spec_links[s];
+        auto it = M.link_id.find(g.link_name);
+        if (it == M.link_id.end()) throw std::invalid_argument("no link named " + g.link_name);
+        g.link = it->second;
+        int n = counts[s];
+        if (n <= 0) throw std::invalid_argument("sphere spec with no spheres");
+        double ctr[3] = {0, 0, 0};
+        for (int j = 0; j < n; j++) {
+          std::array<double, 3> v{rel_xyz[3 * (off + j)], rel_xyz[3 * (off + j) + 1], rel_xyz[3 * (off + j) + 2]};
+          g.rel.push_back(v);
+          g.radii.push_back(radii[off + j]);
+          for (int a = 0; a < 3; a++) ctr[a] = ctr[a] + v[a];
+        }
+        for (int a = 0; a < 3; a++) g.centre[a] = ctr[a] / n;
+        double md = 0.0;
+        for (int j = 0; j < n; j++) {
+          double d0 = g.rel[j][0] - g.centre[0], d1 = g.rel[j][1] - g.centre[1], d2 = g.rel[j][2] - g.centre[2];
+          double d = std::sqrt(d0 * d0 + (d1 * d1 + d2 * d2)) + g.radii[j];
+          if (d > md) md = d;
+        }
+        g.radius = md;
+        g.only_self = only_self ? only_self[s] != 0 : false;
+        off += n;
+        c.groups.push_back(g);
+        if (reorder_spheres) {  // re-applied to every group so far, as the constructor loop does
+          for (auto& gg : c.groups) {
+            auto ord = farthest_order(gg.rel);
+            std::vector<std::array<double, 3>> r2(gg.rel.size());
+            std::vector<double> rad2(gg.rel.size());
+            for (size_t i = 0; i < ord.size(); i++) {
+              r2[i] = gg.rel[ord[i]];
+              rad2[i] = gg.radii[ord[i]];
+            }
+            gg.rel = r2;
+            gg.radii = rad2;
+          }
+        }
+      }
+      for (int p = 0; p < n_pairs; p++) {  // :162-177
+        int a = -1, b = -1;
+        for (size_t k = 0; k < c.groups.size(); k++) {
+          if (a < 0 && c.groups[k].link_name == pair_a[p]) a = (int)k;
+          if (b < 0 && c.groups[k].link_name == pair_b[p]) b = (int)k;
+        }
+        if (a < 0 || b < 0) fail(PMGPU_ERR_RUNTIME, "(cpp) Invalid pair of link names for self collision");
+        c.pairs.push_back({a, b});
+      }
+      if (fixed_sdf) c.fixed_sdf = fixed_sdf->s;
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+void pmgpu_cst_destroy(pmgpu_cst* c) { delete c; }
+int pmgpu_cst_set_sdf(pmgpu_cst* c, pmgpu_sdf* sdf) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    c->c.sdf = sdf ? sdf->s : nullptr;
+  });
+}
+int pmgpu_cst_dims(const pmgpu_cst* c, int* q_dim, int* cst_dim, int* n_spheres, int* n_groups) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    HostCst& C = const_cast<pmgpu_cst*>(c)->c;
+    if (q_dim) *q_dim = C.q_dim();
+    if (cst_dim) *cst_dim = C.cst_dim();
+    if (n_spheres) *n_spheres = C.n_spheres();
+    if (n_groups) *n_groups = (int)C.groups.size();
+  });
+}
+int pmgpu_cst_groups(const pmgpu_cst* c, int32_t* link, double* radius, double* centre3, int32_t* only_self, double* sphere_rel3,
+                     double* sphere_radii) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    size_t k = 0;
+    for (size_t g = 0; g < c->c.groups.size(); g++) {
+      const HostGroup& G = c->c.groups[g];
+      if (link) link[g] = G.link;
+      if (radius) radius[g] = G.radius;
+      if (centre3) std::memcpy(centre3 + 3 * g, G.centre.data(), 24);
+      if (only_self) only_self[g] = G.only_self;
+      for (size_t i = 0; i < G.radii.size(); i++, k++) {
+        if (sphere_rel3) std::memcpy(sphere_rel3 + 3 * k, G.rel[i].data(), 24);
+        if (sphere_radii) sphere_radii[k] = G.radii[i];
+      }
+    }
+  });
+}
+int pmgpu_cst_update_kintree(pmgpu_cst* c, const double* q, int high_accuracy) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    HostCst& C = c->c;
+    C.tables();
+    HostModel& M = *C.kin;
+    int nq = C.q_dim(), nc = (int)C.ids.size();
+    for (int i = 0; i < nc; i++) M.angles[C.ids[i]] = q[i];
+    double* dq = (double*)C.w_aux.ensure((size_t)nq * 8 + 16);
+    cuda_check(cudaMemcpy(dq, q, (size_t)nq * 8, cudaMemcpyHostToDevice), "H2D");
+    // primitive.hpp:38-62: non-FIXED bases always use exact sin/cos for the joints
+    int accurate = (C.base_type != PM_BASE_FIXED) ? 1 : (high_accuracy ? 1 : 0);
+    if (nc > 0) cuda_check(launch_set_joints(M.d_state.as<double>(), C.d_ctrl_recs.as<PmSlot>(), dq, nc, accurate, 0), "update_kintree");
+    if (C.base_type != PM_BASE_FIXED) cuda_check(launch_set_base_from_q(M.d_state.as<double>(), C.base_type, dq + nc, 0), "update_kintree");
+    cuda_check(cudaDeviceSynchronize(), "update_kintree");
+  });
+}
+static int spheres_of_state(pmgpu_cst* c, double* out4, int groups) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    size_t n = groups ? C.groups.size() : (size_t)C.n_spheres();
+    double* d = (double*)C.w_aux.ensure(std::max<size_t>(n * 32, 16));
+    cuda_check(launch_spheres_of_state(T, C.kin->d_state.as<double>(), groups, d, 0), "spheres");
+    cuda_check(cudaMemcpy(out4, d, n * 32, cudaMemcpyDeviceToHost), "D2H");
+  });
+}
+int pmgpu_cst_get_all_spheres(pmgpu_cst* c, double* out4) { return spheres_of_state(c, out4, 0); }
+int pmgpu_cst_get_group_spheres(pmgpu_cst* c, double* out4) { return spheres_of_state(c, out4, 1); }
+
+int pmgpu_cst_is_valid(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_is_valid64(T, st, q, B, out, s), "is_valid");
+      return;
+    }
+    const double* dq = stage_in(C.w_in, q, (size_t)B * C.q_dim(), s);
+    uint8_t* dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)B, 16));
+    cuda_check(launch_is_valid64(T, st, dq, B, dout, s), "is_valid");
+    stage_out(out, dout, (size_t)B, s);
+    cuda_check(cudaStreamSynchronize(s), "is_valid");
+  });
+}
+int pmgpu_cst_evaluate(pmgpu_cst* c, const double* q, int64_t B, double* vals, double* jac, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    int m = C.cst_dim(), d = C.q_dim();
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_evaluate64(T, st, q, B, 1, vals, jac, s), "evaluate");
+      return;
+    }
+    const double* dq = stage_in(C.w_in, q, (size_t)B * d, s);
+    double* dv = (double*)C.w_out.ensure(std::max<size_t>((size_t)B * m * 8, 16));
+    double* dj = (double*)C.w_out2.ensure(std::max<size_t>((size_t)B * m * d * 8, 16));
+    cuda_check(launch_evaluate64(T, st, dq, B, 1, dv, dj, s), "evaluate");
+    stage_out(vals, dv, (size_t)B * m, s);
+    stage_out(jac, dj, (size_t)B * m * d, s);
+    cuda_check(cudaStreamSynchronize(s), "evaluate");
+  });
+}
+int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int high_accuracy, double* dist, double* centres, int mem,
+                               void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    int ns = C.n_spheres();
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_sphere_dist64(T, st, q, B, high_accuracy, dist, centres, s), "sphere distances");
+      return;
+    }
+    const double* dq = stage_in(C.w_in, q, (size_t)B * C.q_dim(), s);
+    double* dd = dist ? (double*)C.w_out.ensure(std::max<size_t>((size_t)B * ns * 8, 16)) : nullptr;
+    double* dc = centres ? (double*)C.w_out2.ensure(std::max<size_t>((size_t)B * ns * 24, 16)) : nullptr;
+    cuda_check(launch_sphere_dist64(T, st, dq, B, high_accuracy, dd, dc, s), "sphere distances");
+    if (dist) stage_out(dist, dd, (size_t)B * ns, s);
+    if (centres) stage_out(centres, dc, (size_t)B * ns * 3, s);
+    cuda_check(cudaStreamSynchronize(s), "sphere distances");
+  });
+}
+int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
+                       double resolution, uint8_t* out, int64_t* n_checked, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (validator_type != PMGPU_VALIDATOR_BOX && validator_type != PMGPU_VALIDATOR_EUCLIDEAN)
+      fail(PMGPU_ERR_RUNTIME, "unknown validator type");
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const int16_t* seq = C.seq_table();
+    int d = C.q_dim();
+    const double* dw = nullptr;
+    if (validator_type == PMGPU_VALIDATOR_BOX) {
+      check_ptr(width, "width");
+      dw = (const double*)C.w_width.ensure((size_t)d * 8 + 16);
+      if (mem == PMGPU_MEM_DEVICE)
+        cuda_check(cudaMemcpyAsync((void*)dw, width, (size_t)d * 8, cudaMemcpyDeviceToDevice, s), "width");
+      else
+        cuda_check(cudaMemcpyAsync((void*)dw, width, (size_t)d * 8, cudaMemcpyHostToDevice, s), "width");
+    }
+    unsigned long long* cnt = (unsigned long long*)C.w_aux.ensure(64);
+    cuda_check(cudaMemsetAsync(cnt, 0, 8, s), "memset");
+    if (mem == PMGPU_MEM_DEVICE) {
+      cuda_check(launch_check_motion64(T, st, s1, s2, E, validator_type, dw, resolution, seq, out, cnt, s), "check_motion");
+      if (n_checked) {
+        unsigned long long h = 0;
+        cuda_check(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaStreamSynchronize(s), "check_motion");
+        *n_checked = (int64_t)h;
+      }
+      return;
+    }
+    const double* d1 = stage_in(C.w_in, s1, (size_t)E * d, s);
+    const double* d2 = stage_in(C.w_in2, s2, (size_t)E * d, s);
+    uint8_t* dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)E, 16));
+    cuda_check(launch_check_motion64(T, st, d1, d2, E, validator_type, dw, resolution, seq, dout, cnt, s), "check_motion");
+    stage_out(out, dout, (size_t)E, s);
+    unsigned long long h = 0;
+    cuda_check(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "check_motion");
+    if (n_checked) *n_checked = (int64_t)h;
+  });
+}
+
+}  // extern "C"

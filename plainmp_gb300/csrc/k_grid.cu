@@ -1,0 +1,232 @@
+// Device construction of the point-cloud grid used in place of the reference KD-tree
+// (collision/kdtree.cpp:20-65).  Steps: fine-cell key per point (cells numbered
+// block-major) -> per-cell counts -> exclusive scan -> scatter -> occupied-cell records with
+// conservative FP32 boxes -> per-block record ranges and boxes.  The order of points inside a
+// cell follows atomic arrival and is not fixed; nearest distances do not depend on it.
+#include <vector>
+
+#include "pm_grid.cuh"
+#include "pm_launch.h"
+
+namespace {
+
+constexpr int SCAN_BS = 1024;
+
+__global__ void k_keys(const double* __restrict__ pts, int64_t n, double ox, double oy, double oz, double inv_cell, int ncx,
+                       int ncy, int ncz, int nbx, int nby, int32_t* __restrict__ key, int32_t* __restrict__ rank,
+                       int32_t* __restrict__ count) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+  double o[3] = {ox, oy, oz};
+  int nc[3] = {ncx, ncy, ncz};
+  int c[3];
+  for (int a = 0; a < 3; a++) {
+    double f = floor((p[a] - o[a]) * inv_cell);
+    c[a] = f < 0 ? 0 : (f > nc[a] - 1 ? nc[a] - 1 : (int)f);
+  }
+  int b = (c[0] / PM_GRID_B) + nbx * ((c[1] / PM_GRID_B) + nby * (c[2] / PM_GRID_B));
+  int l = (c[0] % PM_GRID_B) + PM_GRID_B * ((c[1] % PM_GRID_B) + PM_GRID_B * (c[2] % PM_GRID_B));
+  int k = b * PM_GRID_CELLS_PER_BLOCK + l;
+  key[i] = k;
+  rank[i] = atomicAdd(count + k, 1);
+}
+
+// exclusive scan, phase 1: per-block scan + block sums
+__global__ void k_scan_local(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ out, int32_t* __restrict__ sums) {
+  __shared__ int32_t buf[SCAN_BS];
+  int64_t i = blockIdx.x * (int64_t)SCAN_BS + threadIdx.x;
+  int32_t v = i < n ? in[i] : 0;
+  buf[threadIdx.x] = v;
+  __syncthreads();
+  for (int off = 1; off < SCAN_BS; off <<= 1) {
+    int32_t t = threadIdx.x >= off ? buf[threadIdx.x - off] : 0;
+    __syncthreads();
+    buf[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) out[i] = buf[threadIdx.x] - v;
+  if (threadIdx.x == SCAN_BS - 1) sums[blockIdx.x] = buf[threadIdx.x];
+}
+__global__ void k_scan_add(int32_t* __restrict__ out, int64_t n, const int32_t* __restrict__ offs) {
+  int64_t i = blockIdx.x * (int64_t)SCAN_BS + threadIdx.x;
+  if (i < n) out[i] += offs[blockIdx.x];
+}
+
+// exclusive scan of n int32 into out (out may alias nothing); uses tmp allocations
+cudaError_t exclusive_scan(const int32_t* in, int64_t n, int32_t* out, cudaStream_t s, std::vector<void*>& tmp) {
+  int64_t nb = (n + SCAN_BS - 1) / SCAN_BS;
+  int32_t* sums = nullptr;
+  cudaError_t e = cudaMalloc(&sums, (size_t)(nb + 1) * sizeof(int32_t));
+  if (e != cudaSuccess) return e;
+  tmp.push_back(sums);
+  k_scan_local<<<(unsigned)nb, SCAN_BS, 0, s>>>(in, n, out, sums);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (nb > 1) {
+    int32_t* offs = nullptr;
+    if ((e = cudaMalloc(&offs, (size_t)(nb + 1) * sizeof(int32_t))) != cudaSuccess) return e;
+    tmp.push_back(offs);
+    if ((e = exclusive_scan(sums, nb, offs, s, tmp)) != cudaSuccess) return e;
+    k_scan_add<<<(unsigned)nb, SCAN_BS, 0, s>>>(out, n, offs);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+__global__ void k_scatter(const double* __restrict__ pts, int64_t n, const int32_t* __restrict__ key, const int32_t* __restrict__ rank,
+                          const int32_t* __restrict__ start, double* __restrict__ px, double* __restrict__ py, double* __restrict__ pz,
+                          float4* __restrict__ p32) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int pos = start[key[i]] + rank[i];
+  double x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+  px[pos] = x;
+  py[pos] = y;
+  pz[pos] = z;
+  p32[pos] = make_float4((float)x, (float)y, (float)z, 0.0f);
+}
+
+__global__ void k_flags(const int32_t* __restrict__ count, int64_t nc, int32_t* __restrict__ flag) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < nc) flag[i] = count[i] > 0 ? 1 : 0;
+}
+
+__global__ void k_cell_records(const int32_t* __restrict__ count, const int32_t* __restrict__ start, const int32_t* __restrict__ recidx,
+                               int64_t nc, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
+                               float* __restrict__ cell_box, int32_t* __restrict__ cell_pts) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= nc || count[c] == 0) return;
+  int r = recidx[c];
+  int p0 = start[c], p1 = p0 + count[c];
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = p0; i < p1; i++) {
+    double v[3] = {px[i], py[i], pz[i]};
+    for (int a = 0; a < 3; a++) {
+      lo[a] = fmin(lo[a], v[a]);
+      hi[a] = fmax(hi[a], v[a]);
+    }
+  }
+  for (int a = 0; a < 3; a++) {
+    cell_box[6 * r + a] = __double2float_rd(lo[a]);
+    cell_box[6 * r + 3 + a] = __double2float_ru(hi[a]);
+  }
+  cell_pts[2 * r] = p0;
+  cell_pts[2 * r + 1] = p1;
+}
+
+__global__ void k_block_records(const int32_t* __restrict__ recidx_ex, int64_t nblocks, int32_t n_rec, const float* __restrict__ cell_box,
+                                int32_t* __restrict__ blk_occ, float* __restrict__ blk_box) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  int r0 = recidx_ex[b * PM_GRID_CELLS_PER_BLOCK];
+  int r1 = (b + 1 < nblocks) ? recidx_ex[(b + 1) * PM_GRID_CELLS_PER_BLOCK] : n_rec;
+  blk_occ[2 * b] = r0;
+  blk_occ[2 * b + 1] = r1;
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int r = r0; r < r1; r++)
+    for (int a = 0; a < 3; a++) {
+      lo[a] = fminf(lo[a], cell_box[6 * r + a]);
+      hi[a] = fmaxf(hi[a], cell_box[6 * r + 3 + a]);
+    }
+  for (int a = 0; a < 3; a++) {
+    blk_box[6 * b + a] = lo[a];
+    blk_box[6 * b + 3 + a] = hi[a];
+  }
+}
+
+inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace
+
+namespace pmg {
+
+void grid_free(GridBuild& g) {
+  for (int i = 0; i < g.n_allocs; i++) cudaFree(g.allocs[i]);
+  g.n_allocs = 0;
+}
+
+cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
+  std::vector<void*> tmp;
+  cudaError_t e = cudaSuccess;
+  g.n_allocs = 0;
+  auto keep = [&](size_t bytes, void** p) -> cudaError_t {
+    cudaError_t r = cudaMalloc(p, bytes < 16 ? 16 : bytes);
+    if (r == cudaSuccess) g.allocs[g.n_allocs++] = *p;
+    return r;
+  };
+  auto scratch = [&](size_t bytes, void** p) -> cudaError_t {
+    cudaError_t r = cudaMalloc(p, bytes < 16 ? 16 : bytes);
+    if (r == cudaSuccess) tmp.push_back(*p);
+    return r;
+  };
+  PmGridDev& d = g.dev;
+  const int64_t n = g.n;
+  const int nb[3] = {d.nbx, d.nby, d.nbz};
+  const int nc[3] = {nb[0] * PM_GRID_B, nb[1] * PM_GRID_B, nb[2] * PM_GRID_B};
+  const int64_t nblocks = (int64_t)nb[0] * nb[1] * nb[2];
+  const int64_t ncells = nblocks * PM_GRID_CELLS_PER_BLOCK;
+  int32_t *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *flag = nullptr, *recidx = nullptr;
+  double *px = nullptr, *py = nullptr, *pz = nullptr;
+  float4* p32 = nullptr;
+  int32_t *blk_occ = nullptr, *cell_pts = nullptr;
+  float *blk_box = nullptr, *cell_box = nullptr;
+  int32_t n_rec = 0;
+  do {
+    if ((e = scratch(n * 4, (void**)&key)) != cudaSuccess) break;
+    if ((e = scratch(n * 4, (void**)&rank)) != cudaSuccess) break;
+    if ((e = scratch(ncells * 4, (void**)&count)) != cudaSuccess) break;
+    if ((e = scratch(ncells * 4, (void**)&start)) != cudaSuccess) break;
+    if ((e = scratch(ncells * 4, (void**)&flag)) != cudaSuccess) break;
+    if ((e = scratch(ncells * 4, (void**)&recidx)) != cudaSuccess) break;
+    if ((e = keep(n * 8, (void**)&px)) != cudaSuccess) break;
+    if ((e = keep(n * 8, (void**)&py)) != cudaSuccess) break;
+    if ((e = keep(n * 8, (void**)&pz)) != cudaSuccess) break;
+    if ((e = keep(n * 16, (void**)&p32)) != cudaSuccess) break;
+    if ((e = keep(nblocks * 8, (void**)&blk_occ)) != cudaSuccess) break;
+    if ((e = keep(nblocks * 24, (void**)&blk_box)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(count, 0, ncells * 4, s)) != cudaSuccess) break;
+    if (n > 0) {
+      k_keys<<<nblk(n, 256), 256, 0, s>>>(g.pts, n, d.origin[0], d.origin[1], d.origin[2], 1.0 / g.cell, nc[0], nc[1], nc[2], nb[0],
+                                           nb[1], key, rank, count);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+    }
+    if ((e = exclusive_scan(count, ncells, start, s, tmp)) != cudaSuccess) break;
+    if (n > 0) {
+      k_scatter<<<nblk(n, 256), 256, 0, s>>>(g.pts, n, key, rank, start, px, py, pz, p32);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+    }
+    k_flags<<<nblk(ncells, 256), 256, 0, s>>>(count, ncells, flag);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    if ((e = exclusive_scan(flag, ncells, recidx, s, tmp)) != cudaSuccess) break;
+    int32_t last_idx = 0, last_flag = 0;
+    if ((e = cudaMemcpyAsync(&last_idx, recidx + ncells - 1, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(&last_flag, flag + ncells - 1, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+    n_rec = last_idx + last_flag;
+    if ((e = keep((size_t)n_rec * 24, (void**)&cell_box)) != cudaSuccess) break;
+    if ((e = keep((size_t)n_rec * 8, (void**)&cell_pts)) != cudaSuccess) break;
+    k_cell_records<<<nblk(ncells, 256), 256, 0, s>>>(count, start, recidx, ncells, px, py, pz, cell_box, cell_pts);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    k_block_records<<<nblk(nblocks, 128), 128, 0, s>>>(recidx, nblocks, n_rec, cell_box, blk_occ, blk_box);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    e = cudaStreamSynchronize(s);
+  } while (false);
+  for (void* p : tmp) cudaFree(p);
+  if (e != cudaSuccess) {
+    grid_free(g);
+    return e;
+  }
+  d.px = px;
+  d.py = py;
+  d.pz = pz;
+  d.p32 = p32;
+  d.blk_occ = blk_occ;
+  d.blk_box = blk_box;
+  d.cell_box = cell_box;
+  d.cell_pts = cell_pts;
+  d.seed = nullptr;
+  d.n_points = (int32_t)n;
+  return cudaSuccess;
+}
+
+}  // namespace pmg

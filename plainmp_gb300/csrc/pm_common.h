@@ -1,0 +1,106 @@
+// Shared host/device layout of the flattened constraint tables.
+//
+// A SphereCollisionCst is flattened once into one contiguous device buffer: a header with
+// counts and byte offsets, then FK slots (the links the constraint touches, parents first),
+// control-joint records, sphere groups, spheres in structure-of-arrays form, self pairs and
+// primitive SDF parameter blocks.  The model's mutable state (per-link local transform and
+// base pose) lives in a separate device array so that several constraints share it, like
+// the reference's shared KinematicModel (constraints/primitive.hpp:96).
+#pragma once
+#include <stdint.h>
+
+#define PM_MAX_SLOTS 64   // links one constraint can touch (FK slots)
+#define PM_MAX_CTRL 64    // control joints (relevance bitmask width)
+#define PM_MAX_CLOUDS 8
+#define PM_GRID_B 4  // fine cells per block edge of the point-cloud grid
+#define PM_GRID_CELLS_PER_BLOCK (PM_GRID_B * PM_GRID_B * PM_GRID_B)
+
+enum { PM_FK_STATE = 0, PM_FK_REV = 1, PM_FK_PRIS = 2 };
+enum { PM_BASE_FIXED = 0, PM_BASE_FLOATING = 1, PM_BASE_PLANAR = 2 };
+enum { PM_SDF_UNION = 0, PM_SDF_BOX = 1, PM_SDF_CYLINDER = 2, PM_SDF_SPHERE = 3, PM_SDF_GROUND = 4, PM_SDF_CLOUD = 5 };
+
+// Model state rows of [qx qy qz qw tx ty tz qid] doubles (qid 0/1): row 0 is the base pose,
+// row 1 + link is the link's local transform (tf_plink_to_hlink_cache_, kinematics.hpp:91).
+#define PM_STATE_STRIDE 8
+#define PM_STATE_BASE_ROW 0
+#define PM_STATE_LINK_ROW(link) (1 + (link))
+
+struct PmSlot {
+  int32_t link;             // model link id (row of the state array)
+  int32_t parent;           // parent slot, -1 for the root link (pose = base pose)
+  int32_t mode;             // PM_FK_STATE | PM_FK_REV | PM_FK_PRIS
+  int32_t qcol;             // q column of the control joint (REV/PRIS)
+  int32_t origin_identity;  // joint origin orientation flag |w-1| < 1e-6 (kinematics.cpp:110-113)
+  int32_t pad;
+  uint64_t relevant;        // bit i: control joint i moves this link (rptable, kinematics.cpp:340-363)
+  double axis[3];
+  double oq[4];             // joint origin quaternion x y z w
+  double ot[3];             // joint origin translation
+};
+
+struct PmJoint {  // one per control joint, for Jacobian columns (algorithm.cpp:359-379)
+  int32_t slot;   // slot of the joint's child link, -1 if the constraint never needs it
+  int32_t prismatic;
+  double axis[3];
+};
+
+struct PmGroup {
+  int32_t slot;
+  int32_t begin;  // first sphere
+  int32_t count;
+  int32_t only_self;
+  double rel[3];  // group sphere centre in the link frame
+  double radius;
+};
+
+struct PmPrim {
+  int32_t kind;
+  int32_t axis_aligned;
+  int32_t z_axis_aligned;
+  int32_t cloud;  // index into the cloud table for PM_SDF_CLOUD
+  double lb[3], ub[3];
+  double pos[3];
+  double rot[9];      // row-major
+  double rot_inv[9];  // row-major
+  double a, b, c;     // box: half widths; cylinder: r, r^2, h/2; sphere: r, r^2; ground: h; cloud: radius
+};
+
+// Device view of one point-cloud grid (exact nearest neighbour).  Points are sorted by
+// fine cell; fine cells are numbered block-major (B x B x B cells per block) so the points
+// of one block are contiguous.  Only occupied cells carry a record.
+struct PmGridDev {
+  const double* px;        // sorted points, FP64 SoA
+  const double* py;
+  const double* pz;
+  const float4* p32;       // same points, FP32 (x y z 0)
+  const int32_t* blk_occ;  // per block: [first occupied-cell record, end)
+  const float* blk_box;    // per block: lo xyz, hi xyz (empty: +inf/-inf)
+  const float* cell_box;   // per occupied cell: lo xyz, hi xyz
+  const int32_t* cell_pts; // per occupied cell: [first point, end)
+  const int32_t* seed;     // per block: index of a point near the block (upper-bound seed)
+  int32_t nbx, nby, nbz;   // blocks per axis
+  int32_t n_points;
+  double origin[3];        // grid origin (world)
+  double block;            // block edge length
+  double lb[3], ub[3];     // CloudSDF AABB (point bounds -/+ radius)
+  double radius;
+};
+
+struct PmTablesHdr {
+  int32_t n_slots, n_ctrl, n_groups, n_spheres;
+  int32_t n_pairs, n_prims, q_dim, base_type;
+  int32_t root_slot, n_clouds, pad0, pad1;
+  int64_t off_slots, off_joints, off_groups, off_sx, off_sy, off_sz, off_sr, off_sgroup, off_pairs, off_prims, off_clouds;
+  int64_t total_bytes;
+};
+
+#ifdef __CUDACC__
+#define PM_HD __host__ __device__ __forceinline__
+#else
+#define PM_HD inline
+#endif
+
+template <class T>
+PM_HD const T* pm_at(const PmTablesHdr* h, int64_t off) {
+  return reinterpret_cast<const T*>(reinterpret_cast<const char*>(h) + off);
+}

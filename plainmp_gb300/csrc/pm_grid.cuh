@@ -1,0 +1,178 @@
+// Exact nearest-neighbour queries on the device point-cloud grid (replaces the KD-tree of
+// collision/kdtree.cpp:67-96 inside CloudSDF::evaluate, primitive_sdf.hpp:597-599).
+//
+// Layout (built by k_grid.cu): blocks of PM_GRID_B^3 fine cells; each occupied fine cell has
+// a conservative FP32 bounding box of its points (lo rounded down, hi rounded up) and a
+// contiguous point range; each block has the union box and its range of occupied-cell
+// records.  A query walks Chebyshev rings of blocks around the query's (clamped) block,
+// skips blocks and cells whose box is at least as far as the best distance so far, and
+// stops once every unvisited block lies beyond the best distance.
+//
+// Exactness: the squared distance of a point is fl(dx*dx + (dy*dy + dz*dz)) with d = p - q,
+// as the KD-tree computes it (kdtree.cpp:125).  The box distance uses the same formula on
+// per-axis gaps that are never larger than the gap to any point in the box, and rounding is
+// monotone, so a pruned box holds no point with a smaller squared distance: the returned
+// value is exactly min_i fl(|p_i - q|^2), the KD-tree's value.  Among exactly equidistant
+// points the nearest point returned may differ from the KD-tree's.
+#pragma once
+#include "pm_common.h"
+#include "pm_math.cuh"
+
+
+namespace pmd {
+
+__device__ __forceinline__ double gap64(double q, double lo, double hi) {
+  if (q < lo) return lo - q;
+  if (q > hi) return q - hi;
+  return 0.0;
+}
+__device__ __forceinline__ double box_d2_64(const float* b, const D3& q) {
+  double gx = gap64(q.x, (double)b[0], (double)b[3]);
+  double gy = gap64(q.y, (double)b[1], (double)b[4]);
+  double gz = gap64(q.z, (double)b[2], (double)b[5]);
+  return gx * gx + (gy * gy + gz * gz);
+}
+
+struct NNResult64 {
+  double d2;
+  int32_t idx;  // sorted point index, -1 if the cloud is empty
+};
+
+// Exact FP64 nearest squared distance.  The loop over rings is bounded by the grid size.
+__device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q) {
+  NNResult64 r{INFINITY, -1};
+  if (G.n_points <= 0) return r;
+  const double inv = 1.0 / G.block;
+  int cb[3];
+  const double qa[3] = {q.x, q.y, q.z};
+  const int nb[3] = {G.nbx, G.nby, G.nbz};
+  for (int a = 0; a < 3; a++) {
+    double f = floor((qa[a] - G.origin[a]) * inv);
+    int c = f < 0 ? 0 : (f > nb[a] - 1 ? nb[a] - 1 : (int)f);
+    cb[a] = c;
+  }
+  const int kmax = max(nb[0], max(nb[1], nb[2]));
+  for (int K = 0; K <= kmax; K++) {
+    const int z0 = max(cb[2] - K, 0), z1 = min(cb[2] + K, nb[2] - 1);
+    const int y0 = max(cb[1] - K, 0), y1 = min(cb[1] + K, nb[1] - 1);
+    const int x0 = max(cb[0] - K, 0), x1 = min(cb[0] + K, nb[0] - 1);
+    for (int bz = z0; bz <= z1; bz++) {
+      const bool zf = (bz == cb[2] - K) || (bz == cb[2] + K);
+      for (int by = y0; by <= y1; by++) {
+        const bool yf = zf || (by == cb[1] - K) || (by == cb[1] + K);
+        const int step = yf ? 1 : 2 * K;
+        for (int bx = (yf ? x0 : cb[0] - K); bx <= x1; bx += (step > 0 ? step : 1)) {
+          if (bx < x0) continue;
+          const int b = bx + nb[0] * (by + nb[1] * bz);
+          const int c0 = G.blk_occ[2 * b], c1 = G.blk_occ[2 * b + 1];
+          if (c0 >= c1) continue;
+          if (box_d2_64(G.blk_box + 6 * b, q) >= r.d2) continue;
+          for (int c = c0; c < c1; c++) {
+            if (box_d2_64(G.cell_box + 6 * c, q) >= r.d2) continue;
+            const int p0 = G.cell_pts[2 * c], p1 = G.cell_pts[2 * c + 1];
+            for (int i = p0; i < p1; i++) {
+              D3 d{G.px[i] - q.x, G.py[i] - q.y, G.pz[i] - q.z};
+              double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
+              if (d2 < r.d2) {
+                r.d2 = d2;
+                r.idx = i;
+              }
+            }
+          }
+          if (K == 0) break;
+        }
+      }
+    }
+    // lower bound for blocks outside the visited cube
+    double lb = INFINITY;
+    for (int a = 0; a < 3; a++) {
+      if (cb[a] - K - 1 >= 0) {
+        double face = G.origin[a] + (double)(cb[a] - K) * G.block;
+        lb = fmin(lb, qa[a] - face);
+      }
+      if (cb[a] + K + 1 <= nb[a] - 1) {
+        double face = G.origin[a] + (double)(cb[a] + K + 1) * G.block;
+        lb = fmin(lb, face - qa[a]);
+      }
+    }
+    if (lb == INFINITY) break;  // the cube covers the grid
+    // nominal block faces carry the rounding of the build-time block assignment (~1e-16 m):
+    // stop only when the bound minus 1 nm still clears the best distance
+    const double lbm = lb - 1e-9;
+    if (lbm > 0 && lbm * lbm >= r.d2) break;
+  }
+  return r;
+}
+
+// FP32 variant: same walk in single precision.  Returns the exact minimum over points of the
+// FP32-evaluated squared distance (same monotonicity argument).
+struct NNResult32 {
+  float d2;
+  int32_t idx;
+};
+__device__ __forceinline__ float gap32(float q, float lo, float hi) { return fmaxf(fmaxf(lo - q, q - hi), 0.0f); }
+__device__ __forceinline__ float box_d2_32(const float* b, float qx, float qy, float qz) {
+  float gx = gap32(qx, b[0], b[3]), gy = gap32(qy, b[1], b[4]), gz = gap32(qz, b[2], b[5]);
+  return fmaf(gx, gx, fmaf(gy, gy, gz * gz));
+}
+__device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float qy, float qz) {
+  NNResult32 r{INFINITY, -1};
+  if (G.n_points <= 0) return r;
+  const float inv = (float)(1.0 / G.block);
+  const float ox = (float)G.origin[0], oy = (float)G.origin[1], oz = (float)G.origin[2];
+  const float blk = (float)G.block;
+  const float qa[3] = {qx, qy, qz};
+  const float oa[3] = {ox, oy, oz};
+  const int nb[3] = {G.nbx, G.nby, G.nbz};
+  int cb[3];
+  for (int a = 0; a < 3; a++) {
+    float f = floorf((qa[a] - oa[a]) * inv);
+    cb[a] = f < 0.f ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
+  }
+  const int kmax = max(nb[0], max(nb[1], nb[2]));
+  for (int K = 0; K <= kmax; K++) {
+    const int z0 = max(cb[2] - K, 0), z1 = min(cb[2] + K, nb[2] - 1);
+    const int y0 = max(cb[1] - K, 0), y1 = min(cb[1] + K, nb[1] - 1);
+    const int x0 = max(cb[0] - K, 0), x1 = min(cb[0] + K, nb[0] - 1);
+    for (int bz = z0; bz <= z1; bz++) {
+      const bool zf = (bz == cb[2] - K) || (bz == cb[2] + K);
+      for (int by = y0; by <= y1; by++) {
+        const bool yf = zf || (by == cb[1] - K) || (by == cb[1] + K);
+        const int step = yf ? 1 : 2 * K;
+        for (int bx = (yf ? x0 : cb[0] - K); bx <= x1; bx += (step > 0 ? step : 1)) {
+          if (bx < x0) continue;
+          const int b = bx + nb[0] * (by + nb[1] * bz);
+          const int2 occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + b);
+          if (occ.x >= occ.y) continue;
+          if (box_d2_32(G.blk_box + 6 * b, qx, qy, qz) >= r.d2) continue;
+          for (int c = occ.x; c < occ.y; c++) {
+            if (box_d2_32(G.cell_box + 6 * c, qx, qy, qz) >= r.d2) continue;
+            const int2 pr = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + c);
+            for (int i = pr.x; i < pr.y; i++) {
+              float4 p = __ldg(G.p32 + i);
+              float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+              float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (d2 < r.d2) {
+                r.d2 = d2;
+                r.idx = i;
+              }
+            }
+          }
+          if (K == 0) break;
+        }
+      }
+    }
+    float lb = INFINITY;
+    for (int a = 0; a < 3; a++) {
+      if (cb[a] - K - 1 >= 0) lb = fminf(lb, qa[a] - (oa[a] + (float)(cb[a] - K) * blk));
+      if (cb[a] + K + 1 <= nb[a] - 1) lb = fminf(lb, (oa[a] + (float)(cb[a] + K + 1) * blk) - qa[a]);
+    }
+    if (lb == INFINITY) break;
+    // face positions carry FP32 rounding (< 1e-6 m inside a few-metre workspace)
+    const float lbm = lb - 4e-6f;
+    if (lbm > 0.f && lbm * lbm >= r.d2) break;
+  }
+  return r;
+}
+
+}  // namespace pmd

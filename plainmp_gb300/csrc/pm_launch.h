@@ -1,0 +1,58 @@
+// Host-side launchers of the device kernels (implemented in the .cu translation units).
+// All pointers are device pointers; every launcher enqueues on `stream` and returns the
+// launch status.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pm_common.h"
+
+namespace pmg {
+
+// ---- model state (k_plain.cu)
+// recs: per joint to set, a PmSlot whose `link` is the child link and mode REV/PRIS.
+cudaError_t launch_set_joints(double* state, const PmSlot* recs, const double* q, int n, int accurate, cudaStream_t s);
+// base pose from q for PLANAR/FLOATING (q points at the base part), written to row 0.
+cudaError_t launch_set_base_from_q(double* state, int base_type, const double* qbase, cudaStream_t s);
+// link poses of the current state: parents[n_link] (-1 root), links[n] -> out7[n*7]
+cudaError_t launch_link_poses(const double* state, const int32_t* parents, const int32_t* links, int n, double* out7,
+                              cudaStream_t s);
+
+// ---- constraint batches (k_plain.cu)
+cudaError_t launch_is_valid64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, uint8_t* out,
+                              cudaStream_t s);
+cudaError_t launch_evaluate64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int high_accuracy,
+                              double* vals, double* jac, cudaStream_t s);
+cudaError_t launch_sphere_dist64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int high_accuracy,
+                                 double* dist, double* centres, cudaStream_t s);
+// spheres (all: groups=0, group spheres: groups=1) of the current state, out4 n x 4
+cudaError_t launch_spheres_of_state(const PmTablesHdr* T, const double* state, int groups, double* out4, cudaStream_t s);
+// checkMotion over E edges; seq: 128 x 128 int16 sequence table; width: q_dim (box) or NULL
+cudaError_t launch_check_motion64(const PmTablesHdr* T, const double* state, const double* s1, const double* s2, int64_t E,
+                                  int type, const double* width, double resolution, const int16_t* seq, uint8_t* out,
+                                  unsigned long long* n_checked, cudaStream_t s);
+
+// ---- SDF utilities (k_plain.cu): prims/clouds describe one SDF (a union is flattened)
+cudaError_t launch_sdf_points(const PmPrim* prims, int n_prims, const PmGridDev* clouds, int is_union, const double* pts,
+                              const double* radii, int64_t n, double* eval_out, uint8_t* outside_out, cudaStream_t s);
+cudaError_t launch_cloud_nearest(const PmGridDev* grid, const double* pts, int64_t n, double* sq, double* near3,
+                                 cudaStream_t s);
+
+// ---- point-cloud grid build (k_grid.cu)
+struct GridBuild {
+  // inputs
+  const double* pts;  // device, n x 3
+  int64_t n;
+  double radius;
+  double cell;  // fine cell edge
+  // outputs (owned by the caller after the call; freed with grid_free)
+  PmGridDev dev;
+  void* allocs[16];
+  int n_allocs;
+};
+// Builds the grid synchronously on `s` (allocates device memory); returns cudaSuccess or the
+// first CUDA error.  host_lb/host_ub receive the CloudSDF AABB.
+cudaError_t grid_build(GridBuild& g, cudaStream_t s);
+void grid_free(GridBuild& g);
+
+}  // namespace pmg

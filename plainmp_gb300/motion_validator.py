@@ -1,0 +1,85 @@
+"""Motion validators mirroring plainmp's OMPL validators (cpp/plainmp/ompl/motion_validator.hpp:22-63):
+``BoxMotionValidator(width)`` and ``EuclideanMotionValidator(resolution)``, both answering
+``checkMotion(s1, s2)`` against an inequality constraint.  ``check_motion_batch`` is the
+device hot path over E edges."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from ._lib import Batch, check, f64, lib
+from .constraint import SphereCollisionCst
+
+BOX = 0
+EUCLIDEAN = 1
+
+
+class _ValidatorBase:
+    kind = BOX
+
+    def __init__(self, cst: SphereCollisionCst) -> None:
+        self.cst = cst
+        self._width = np.zeros(cst.q_dim())
+        self._res = 0.0
+
+    def _edges(self, S1, S2):
+        b1, b2 = Batch(S1), Batch(S2)
+        d = self.cst.q_dim()
+        if b1.shape != b2.shape or len(b1.shape) != 2 or b1.shape[1] != d:
+            raise ValueError(f"s1 and s2 must both be (E, {d})")
+        if b1.mem != b2.mem:
+            raise ValueError("s1 and s2 must live in the same memory space")
+        return b1, b2
+
+    def check_motion_batch(self, S1, S2, return_count: bool = False):
+        """Plain FP64 method, one device thread per edge: (E,) uint8."""
+        b1, b2 = self._edges(S1, S2)
+        E = b1.shape[0]
+        out, optr = b1.empty((E,), np.uint8)
+        w = Batch(self._width) if b1.mem == 0 else Batch(_to_device_like(self._width, b1))
+        cnt = C.c_int64(0)
+        check(lib.pmgpu_check_motion(self.cst._h, b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res), optr, C.byref(cnt), b1.mem,
+                                     b1.stream))
+        return (out, int(cnt.value)) if return_count else out
+
+    def check_motion_fast(self, S1, S2, stats: bool = False):
+        """FP32 + FP64-recheck persistent work-queue path: (E,) uint8 identical to the plain method."""
+        b1, b2 = self._edges(S1, S2)
+        E = b1.shape[0]
+        out, optr = b1.empty((E,), np.uint8)
+        w = Batch(self._width) if b1.mem == 0 else Batch(_to_device_like(self._width, b1))
+        st = np.zeros(4, dtype=np.int64)
+        check(lib.pmgpu_check_motion_fast(self.cst._h, b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res), optr,
+                                          C.c_void_p(st.ctypes.data), b1.mem, b1.stream))
+        if stats:
+            return out, {"waypoints": int(st[0]), "rechecked_terms": int(st[1]), "edges": int(st[2])}
+        return out
+
+    def checkMotion(self, s1, s2) -> bool:  # noqa: N802 (OMPL's name)
+        d = self.cst.q_dim()
+        return bool(self.check_motion_batch(f64(s1, (1, d)), f64(s2, (1, d)))[0])
+
+
+def _to_device_like(arr: np.ndarray, b: Batch):
+    return b.torch.as_tensor(arr, dtype=b.torch.float64, device=b.keep.device)
+
+
+class BoxMotionValidator(_ValidatorBase):
+    kind = BOX
+
+    def __init__(self, cst: SphereCollisionCst, width: Sequence[float]) -> None:
+        super().__init__(cst)
+        w = f64(width).reshape(-1)
+        if w.shape[0] != cst.q_dim():
+            raise RuntimeError("box dimension and space dimension mismatch")
+        self._width = w
+
+
+class EuclideanMotionValidator(_ValidatorBase):
+    kind = EUCLIDEAN
+
+    def __init__(self, cst: SphereCollisionCst, resolution: float) -> None:
+        super().__init__(cst)
+        self._res = float(resolution)

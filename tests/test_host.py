@@ -1,0 +1,190 @@
+"""CPU tests of the product's host side: the C ABI library loads and exports every symbol that
+include/pmgpu.h declares; the C++ URDF reader and tree numbering match the reference's
+urdfdom parser (golden dumps); constraint construction (group spheres, farthest-first
+reorder, pairs) and SDF construction (pose flags, AABBs) match the oracle bit for bit; errors
+map to the reference's exception types.  No compute call runs here."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import golden, plainmp_numbering, rpy_matrix
+
+REPO = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    txt = "\n".join(p.read_text() for p in (REPO / "include").glob("*.h"))
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(pmgpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from plainmp_gb300 import _lib
+
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    syms = declared_symbols()
+    assert len(syms) > 40
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_product_path_has_no_oracle_dependency():
+    pat = re.compile(r"^\s*(from\s+oracle|import\s+oracle)|pyoracle|liboracle|orc_", re.M)
+    for p in list((REPO / "plainmp_gb300").rglob("*.py")) + list((REPO / "plainmp_gb300" / "csrc").glob("*")):
+        assert not pat.search(p.read_text()), p
+
+
+@pytest.mark.parametrize("name", ["chain7", "dualarm", "edge"])
+def test_urdf_reader_matches_urdfdom(name):
+    from plainmp_gb300 import KinematicModel
+
+    g = golden(f"urdf_{name}.json")
+    order, parent, jorder = plainmp_numbering(g)
+    kin = KinematicModel(g["urdf"])
+    st = kin.structure()
+    assert st["link_names"] == order
+    assert list(st["link_parent"]) == parent
+    assert st["joint_names"] == jorder
+    for k, jn in enumerate(jorder):
+        j = g["joints"][jn]
+        assert st["joint_child"][k] == order.index(j["child"])
+        assert st["joint_type"][k] == j["type"]
+        assert list(st["joint_axis"][k]) == j["axis"]
+        lo, hi = kin.get_joint_position_limits([k])[0]
+        if j["type"] == 2:
+            assert lo == -np.inf and hi == np.inf
+        else:
+            assert [lo, hi] == j["limits"]
+    for jn, j in g["joints"].items():
+        li = order.index(j["child"])
+        assert list(st["link_tf7"][li][:3]) == j["xyz"]
+        assert list(st["link_tf7"][li][3:]) == j["quat"]  # rpy -> quaternion -> normalise, bit for bit
+
+
+@pytest.mark.parametrize("name", ["chain7", "dualarm", "edge"])
+def test_urdf_reader_matches_oracle(oracle, name):
+    from plainmp_gb300 import KinematicModel
+
+    g = golden(f"urdf_{name}.json")
+    a = KinematicModel(g["urdf"]).structure()
+    b = oracle.Model(g["urdf"]).structure()
+    assert np.array_equal(a["link_parent"], b["link_parent"])
+    assert np.array_equal(a["link_tf7"], b["link_tf7"])
+    assert np.array_equal(a["link_tf_qid"], b["link_tf_qid"])
+    assert np.array_equal(a["joint_child"], b["joint_child"])
+    assert np.array_equal(a["joint_origin_qid"], b["joint_origin_qid"])
+
+
+def test_urdf_errors():
+    from plainmp_gb300 import KinematicModel
+
+    with pytest.raises(RuntimeError):
+        KinematicModel("")
+    with pytest.raises(RuntimeError):
+        KinematicModel("<robot name='x'><link name='a'/><link name='b'/></robot>")  # two roots
+    with pytest.raises(RuntimeError):
+        KinematicModel("<robot name='x'><link name='a'/><joint name='j' type='revolute'><parent link='a'/>"
+                       "<child link='zz'/><limit lower='0' upper='1'/></joint></robot>")
+    with pytest.raises(RuntimeError):
+        KinematicModel("<robot name='x'><link name='a'/><link name='b'/><joint name='j' type='revolute'><parent link='a'/>"
+                       "<child link='b'/></joint></robot>")  # revolute without limits
+    with pytest.raises(RuntimeError):
+        KinematicModel("<robot><link name='a'/><joint name='j' type='fixed'><origin xyz='1 2'/></joint></robot>")
+    kin = KinematicModel(golden("urdf_chain7.json")["urdf"])
+    with pytest.raises(ValueError):
+        kin.get_joint_ids(["nope"])
+    with pytest.raises(ValueError):
+        kin.get_link_ids(["nope"])
+
+
+def _specs(robot):
+    from plainmp_gb300 import SphereAttachmentSpec
+
+    return [SphereAttachmentSpec(s.parent_link_name, s.relative_positions, s.radii, s.only_self_collision) for s in robot.spheres]
+
+
+@pytest.mark.parametrize("which", ["chain7", "dualarm"])
+@pytest.mark.parametrize("reorder", [True, False])
+def test_constraint_tables_match_oracle(oracle, which, reorder):
+    from plainmp_gb300 import BaseType, KinematicModel, SphereCollisionCst
+    from plainmp_gb300 import workloads as W
+
+    robot = W.chain7_robot() if which == "chain7" else W.dualarm_robot()
+    kin = KinematicModel(robot.urdf)
+    c = SphereCollisionCst(kin, robot.control_joints, BaseType.FIXED, _specs(robot), robot.self_pairs, None, reorder)
+    om = oracle.Model(robot.urdf)
+    oc = oracle.Cst(om, robot.control_joints, 0, robot.spheres, robot.self_pairs, None, reorder)
+    a, b = c.groups(), oc.groups()
+    for k in ("link", "radius", "centre", "only_self", "rel", "radii"):
+        assert np.array_equal(a[k], b[k]), k
+    assert c.q_dim() == oc.q_dim and c.n_spheres == oc.n_spheres
+    assert c.cst_dim() == 1  # self pairs only (no SDF yet)
+
+
+def test_constraint_errors():
+    from plainmp_gb300 import BaseType, KinematicModel, SphereCollisionCst
+    from plainmp_gb300 import workloads as W
+
+    robot = W.chain7_robot()
+    kin = KinematicModel(robot.urdf)
+    with pytest.raises(ValueError):
+        SphereCollisionCst(kin, ["j1", "nope"], BaseType.FIXED, _specs(robot), [], None, True)
+    with pytest.raises(RuntimeError, match="Invalid pair"):
+        SphereCollisionCst(kin, robot.control_joints, BaseType.FIXED, _specs(robot), [("link1", "nolink")], None, True)
+
+
+def test_sdf_construction_matches_oracle(oracle):
+    from plainmp_gb300 import BoxSDF, CylinderSDF, GroundSDF, Pose, SphereSDF, UnionSDF
+
+    rng = np.random.default_rng(0)
+    for i in range(30):
+        pos = rng.standard_normal(3)
+        R = np.eye(3) if i == 0 else (rpy_matrix(0.3, 0, 0) if i == 1 else rpy_matrix(*rng.standard_normal(3)))
+        pairs = [
+            (BoxSDF([0.5, 0.3, 0.6], Pose(pos, R)), oracle.Sdf.box([0.5, 0.3, 0.6], pos, R)),
+            (CylinderSDF(0.7, 0.2, Pose(pos, R)), oracle.Sdf.cylinder(0.7, 0.2, pos, R)),
+            (SphereSDF(0.5, Pose(pos, R)), oracle.Sdf.sphere(0.5, pos, R)),
+        ]
+        for mine, ref in pairs:
+            lb, ub, aa, za = ref.info()
+            assert np.array_equal(mine.lb, lb) and np.array_equal(mine.ub, ub)
+            assert mine.pose.axis_aligned == aa and mine.pose.z_axis_aligned == za
+            t = rng.standard_normal(3)
+            a = float(rng.standard_normal())
+            mine.translate(t)
+            ref.translate(t)
+            mine.rotate_z(a)
+            ref.rotate_z(a)
+            lb, ub, aa, za = ref.info()
+            assert np.array_equal(mine.lb, lb) and np.array_equal(mine.ub, ub)
+    g = GroundSDF(1.0)
+    assert list(g.lb[2:]) == [0.0] and list(g.ub[2:]) == [0.0]
+    with pytest.raises(RuntimeError):
+        g.translate([1, 0, 0])
+    u = UnionSDF([BoxSDF([1, 1, 1], Pose())])
+    u.translate([1.0, 2.0, 3.0])  # members are shared, translated in place
+
+
+def test_pose_flags_known_answers():  # tests/test_psdf.py:27-39
+    from plainmp_gb300 import Pose
+
+    assert Pose(np.zeros(3), np.eye(3)).axis_aligned
+    p2 = Pose(np.zeros(3), rpy_matrix(0.3, 0.0, 0.0))
+    assert not p2.axis_aligned and p2.z_axis_aligned
+    p3 = Pose(np.zeros(3), rpy_matrix(0.3, 0.3, 0.3))
+    assert not p3.axis_aligned and not p3.z_axis_aligned
+
+
+def test_batch_calls_fail_loudly_without_gpu():
+    from plainmp_gb300 import CudaError, device_count
+    from plainmp_gb300 import scenes
+    from plainmp_gb300 import workloads as W
+
+    if device_count() > 0:
+        pytest.skip("a GPU is present")
+    kin, cst, _ = scenes.make_constraint(W.chain7_robot(), W.chain7_scene())
+    with pytest.raises(CudaError):
+        cst.is_valid_batch(W.chain7_configs(4))
