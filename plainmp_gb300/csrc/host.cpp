@@ -551,11 +551,15 @@ struct HostCst {
   std::vector<std::pair<const HostSdf*, uint64_t>> sig;
   uint64_t sig_model_version = 0;
   std::vector<std::shared_ptr<HostSdf>> flat;
+  PmTablesHdr hdr{};  // host copy of the device table header
+  int fast_cpb = 32;  // configurations per block of the fast kernel
   std::vector<int> slot_of_link;
   std::vector<PmSlot> ctrl_recs;  // per control joint (child link, REV/PRIS) for state updates
   DevBuf d_ctrl_recs;
   // workspaces for host-memory calls
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
+  DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
+  DevBuf e_sr, e_n, e_off;            // fast edge path: step ratios, waypoint counts and offsets
   std::vector<int16_t> seq_host;
 
   int q_dim() const { return (int)ids.size() + (base_type == PM_BASE_FLOATING) * 6 + (base_type == PM_BASE_PLANAR) * 3; }
@@ -715,6 +719,7 @@ struct HostCst {
     align();
     h.total_bytes = (int64_t)buf.size();
     std::memcpy(buf.data(), &h, sizeof(h));
+    hdr = h;
     d_tables.release();
     d_tables.ensure(buf.size());
     cuda_check(cudaMemcpy(d_tables.p, buf.data(), buf.size(), cudaMemcpyHostToDevice), "tables upload");
@@ -1503,6 +1508,50 @@ int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int hig
     cuda_check(cudaStreamSynchronize(s), "sphere distances");
   });
 }
+int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats, int mem,
+                            void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(4 * B, 1 << 16), (int64_t)1 << 28);
+    int4* items = (int4*)C.f_items.ensure((size_t)cap * sizeof(int4));
+    char* ctl = (char*)C.f_ctl.ensure(64);
+    unsigned int* count = (unsigned int*)ctl;
+    unsigned long long* dstats = (unsigned long long*)(ctl + 16);
+    uint8_t* ovf = (uint8_t*)C.f_overflow.ensure(std::max<size_t>((size_t)B, 16));
+    cuda_check(cudaMemsetAsync(ctl, 0, 64, s), "memset");
+    cuda_check(cudaMemsetAsync(ovf, 0, std::max<size_t>((size_t)B, 16), s), "memset");
+    const double* dq = q;
+    uint8_t* dout = out;
+    float* dd = dist32;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(C.w_in, q, (size_t)B * C.q_dim(), s);
+      dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)B, 16));
+      dd = dist32 ? (float*)C.w_out2.ensure(std::max<size_t>((size_t)B * C.n_spheres() * 4, 16)) : nullptr;
+    }
+    cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, s), "is_valid_fast");
+    if (mem == PMGPU_MEM_HOST) {
+      stage_out(out, dout, (size_t)B, s);
+      if (dist32) stage_out(dist32, dd, (size_t)B * C.n_spheres(), s);
+    }
+    if (stats || mem == PMGPU_MEM_HOST) {
+      unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+      cuda_check(cudaMemcpyAsync(h, ctl, 48, cudaMemcpyDeviceToHost, s), "D2H");
+      cuda_check(cudaStreamSynchronize(s), "is_valid_fast");
+      if (stats) {
+        stats[0] = B;
+        stats[1] = (int64_t)(unsigned)h[0];
+        stats[2] = (int64_t)h[2 + 2];
+        stats[3] = 0;
+      }
+    }
+  });
+}
 int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
                        double resolution, uint8_t* out, int64_t* n_checked, int mem, void* stream) {
   return guarded([&] {
@@ -1546,6 +1595,78 @@ int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t
     cuda_check(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, s), "D2H");
     cuda_check(cudaStreamSynchronize(s), "check_motion");
     if (n_checked) *n_checked = (int64_t)h;
+  });
+}
+
+int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
+                            double resolution, uint8_t* out, int64_t* stats, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (validator_type != PMGPU_VALIDATOR_BOX && validator_type != PMGPU_VALIDATOR_EUCLIDEAN)
+      fail(PMGPU_ERR_RUNTIME, "unknown validator type");
+    if (E < 0) throw std::invalid_argument("negative edge count");
+    HostCst& C = c->c;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const int16_t* seq = C.seq_table();
+    const int d = C.q_dim();
+    const double* dw = nullptr;
+    if (validator_type == PMGPU_VALIDATOR_BOX) {
+      check_ptr(width, "width");
+      dw = (const double*)C.w_width.ensure((size_t)d * 8 + 16);
+      cuda_check(cudaMemcpyAsync((void*)dw, width, (size_t)d * 8, mem == PMGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
+                 "width");
+    }
+    const size_t En = (size_t)std::max<int64_t>(E, 1);
+    double* sr = (double*)C.e_sr.ensure(En * 8);
+    int32_t* n = (int32_t*)C.e_n.ensure(En * 4);
+    int64_t* off = (int64_t*)C.e_off.ensure(En * 8);
+    const unsigned cap = 1u << 18;
+    int4* items = (int4*)C.f_items.ensure((size_t)cap * sizeof(int4));
+    char* ctl = (char*)C.f_ctl.ensure(64);
+    unsigned int* count = (unsigned int*)ctl;
+    unsigned long long* next = (unsigned long long*)(ctl + 8);
+    unsigned long long* dstats = (unsigned long long*)(ctl + 16);
+    uint8_t* ovf = (uint8_t*)C.f_overflow.ensure(std::max<size_t>(En, 16));
+    cuda_check(cudaMemsetAsync(ctl, 0, 64, s), "memset");
+    cuda_check(cudaMemsetAsync(ovf, 0, std::max<size_t>(En, 16), s), "memset");
+    const double* d1 = s1;
+    const double* d2 = s2;
+    uint8_t* dout = out;
+    if (mem == PMGPU_MEM_HOST) {
+      d1 = stage_in(C.w_in, s1, (size_t)E * d, s);
+      d2 = stage_in(C.w_in2, s2, (size_t)E * d, s);
+      dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)E, 16));
+    }
+    static int n_sm = 0;
+    if (n_sm == 0) {
+      int dev = 0;
+      cuda_check(cudaGetDevice(&dev), "device");
+      cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    }
+    cuda_check(launch_fast_edges(T, C.hdr, st, d1, d2, E, validator_type, dw, resolution, seq, sr, n, off, next, dout, items, count, cap,
+                                 ovf, dstats, 32, n_sm, s),
+               "check_motion_fast");
+    if (mem == PMGPU_MEM_HOST) stage_out(out, dout, (size_t)E, s);
+    if (stats || mem == PMGPU_MEM_HOST) {
+      unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+      int64_t last_off = 0;
+      int32_t last_n = 0;
+      cuda_check(cudaMemcpyAsync(h, ctl, 48, cudaMemcpyDeviceToHost, s), "D2H");
+      if (E > 0) {
+        cuda_check(cudaMemcpyAsync(&last_off, off + E - 1, 8, cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaMemcpyAsync(&last_n, n + E - 1, 4, cudaMemcpyDeviceToHost, s), "D2H");
+      }
+      cuda_check(cudaStreamSynchronize(s), "check_motion_fast");
+      if (stats) {
+        stats[0] = E > 0 ? last_off + last_n : 0;
+        stats[1] = (int64_t)(unsigned)h[0];
+        stats[2] = (int64_t)h[4];
+        stats[3] = 0;
+      }
+    }
   });
 }
 

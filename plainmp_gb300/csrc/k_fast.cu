@@ -1,11 +1,642 @@
-// FP32 fast path with FP64 recheck (filled in by the fast-path kernels).
+// FP32 fast path with FP64 recheck (validity booleans identical to the plain method).
+//
+// Per block of CPB configurations:
+//   1. FK in FP64 (the plain path's exact arithmetic), each slot's rotation matrix and
+//      translation rounded once to FP32 into shared memory;
+//   2. group culling: the clearance of each sphere group's bounding sphere against each
+//      primitive (a point cloud: a radius-bounded FP32 nearest-neighbour query);
+//   3. sphere tasks (sphere x primitive) and self-pair tasks (group pair x sphere pairs), each
+//      decision a tri-state of an FP32 clearance g against a margin m derived from the FP32
+//      error bound: pass if g > m, fail if g < -m, otherwise the term is queued;
+//   4. k_fast_recheck evaluates every queued term with the exact FP64 gate-and-test of the
+//      reference (primitive_sphere_collision.cpp:191-254) and clears the configuration if the
+//      term collides.
+// Why the terms suffice: ext collision = OR over groups g and primitives p of
+// [gate(g,p) AND OR_s test(s,p)] = OR over (s,p) of [gate(g(s),p) AND test(s,p)]; a sphere
+// that certainly collides by more than the margin lies inside its group sphere, whose gate then
+// also fails, so certain terms need no FP64 work.  Self pairs factor the same way.
 #include "pm_launch.h"
-#include "pmgpu.h"
+#include "pm_view.cuh"
 
-extern "C" {
-int pmgpu_cst_is_valid_fast(pmgpu_cst*, const double*, int64_t, uint8_t*, float*, int64_t*, int, void*) { return PMGPU_ERR_RUNTIME; }
-int pmgpu_check_motion_fast(pmgpu_cst*, const double*, const double*, int64_t, int, const double*, double, uint8_t*, int64_t*, int,
-                            void*) {
-  return PMGPU_ERR_RUNTIME;
+using namespace pmd;
+
+namespace {
+
+constexpr float kU = 5.9604645e-8f;  // 2^-24
+// Margin of an FP32 clearance: 64 units of roundoff of the magnitudes involved, plus 1 um.  The
+// error analysis of the FP32 evaluation (pose rounding, one dot product, one square root)
+// gives about 52 units for the box, the largest case.
+__device__ __forceinline__ float margin32(float mag) { return 1e-6f + 64.0f * kU * (1.0f + mag); }
+
+struct PrimF {
+  int kind, aa, za, cloud;
+  float lb[3], ub[3], pos[3], rot[9];
+  float a, b, c, mag;
+};
+struct SphereF {
+  float x, y, z, r;
+  int group, tiny;  // tiny: the FP64 radius is below 1e-6 (the reference's special cases)
+};
+struct GroupF {
+  float rel[3], radius;
+  int slot, begin, count, only_self;
+  int tiny, pad[3];
+};
+
+enum { ST_PASS = 0, ST_FAIL = 1, ST_MAYBE = 2 };
+constexpr int FLAG_FAIL = 1;
+
+struct Scratch {
+  int4* items;
+  unsigned int* count;
+  unsigned int cap;
+  uint8_t* overflow;
+  unsigned long long* stats;
+};
+
+__device__ __forceinline__ float3 xf(const float* P, float x, float y, float z) {  // R (row-major 9) * v + t (P[9..11])
+  return make_float3(fmaf(P[0], x, fmaf(P[1], y, fmaf(P[2], z, P[9]))), fmaf(P[3], x, fmaf(P[4], y, fmaf(P[5], z, P[10]))),
+                     fmaf(P[6], x, fmaf(P[7], y, fmaf(P[8], z, P[11]))));
 }
+
+// Clearance g (the reference reports a collision iff g <= 0, up to its own rounding), the
+// evaluate()-based signed distance sd (minus r) and the magnitude for the margin.
+__device__ __forceinline__ void clearance(const PrimF& P, const PmGridDev* clouds, float cx, float cy, float cz, float r, bool tiny,
+                                          float extra, float& g, float& sd, float& mag) {
+  const float dx = cx - P.pos[0], dy = cy - P.pos[1], dz = cz - P.pos[2];
+  mag = fabsf(cx) + fabsf(cy) + fabsf(cz) + P.mag;
+  switch (P.kind) {
+    case PM_SDF_BOX: {
+      float lx, ly, lz;
+      if (P.aa) {
+        lx = dx;
+        ly = dy;
+        lz = dz;
+      } else {
+        lx = fmaf(dx, P.rot[0], fmaf(dy, P.rot[3], dz * P.rot[6]));
+        ly = fmaf(dx, P.rot[1], fmaf(dy, P.rot[4], dz * P.rot[7]));
+        lz = fmaf(dx, P.rot[2], fmaf(dy, P.rot[5], dz * P.rot[8]));
+      }
+      const float sx = fabsf(lx) - P.a, sy = fabsf(ly) - P.b, sz = fabsf(lz) - P.c;
+      const float mx = fmaxf(sx, 0.f), my = fmaxf(sy, 0.f), mz = fmaxf(sz, 0.f);
+      const float ext = sqrtf(fmaf(mx, mx, fmaf(my, my, mz * mz)));
+      const float ms = fmaxf(sx, fmaxf(sy, sz));
+      g = tiny ? ms - r : ext - r;
+      sd = ext + fminf(ms, 0.f) - r;
+      return;
+    }
+    case PM_SDF_CYLINDER: {
+      float lx, ly, lz;
+      if (P.za) {
+        lx = dx;
+        ly = dy;
+        lz = dz;
+      } else {
+        lx = fmaf(dx, P.rot[0], fmaf(dy, P.rot[3], dz * P.rot[6]));
+        ly = fmaf(dx, P.rot[1], fmaf(dy, P.rot[4], dz * P.rot[7]));
+        lz = fmaf(dx, P.rot[2], fmaf(dy, P.rot[5], dz * P.rot[8]));
+      }
+      const float zs = fabsf(lz) - P.c;
+      const float rs = sqrtf(fmaf(lx, lx, ly * ly)) - P.a;
+      const float a = fmaxf(rs, 0.f), b = fmaxf(zs, 0.f);
+      const float ext = sqrtf(fmaf(a, a, b * b));
+      g = tiny ? fmaxf(zs - r, rs) : ext - r;
+      sd = ext + fminf(fmaxf(rs, zs), 0.f) - r;
+      return;
+    }
+    case PM_SDF_SPHERE: {
+      const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - P.a;
+      g = tiny ? d : d - r;
+      sd = d - r;
+      return;
+    }
+    case PM_SDF_GROUND: {  // the reference's AABB (z in [0, 0]) is part of its decision
+      g = fmaxf(fabsf(cz) - r, cz + P.a - r);
+      sd = cz + P.a - r;
+      return;
+    }
+    case PM_SDF_CLOUD: {
+      const float reach = P.a + r + extra;
+      NNResult32 nn = grid_nearest32(clouds[P.cloud], cx, cy, cz, reach * reach);
+      if (nn.idx < 0) {
+        g = reach - P.a - r;  // nothing closer than reach
+        sd = 3.0e38f;
+        mag = fabsf(cx) + fabsf(cy) + fabsf(cz);
+        return;
+      }
+      const float d = sqrtf(nn.d2);
+      g = d - P.a - r;
+      sd = g;
+      mag = fabsf(cx) + fabsf(cy) + fabsf(cz) + d;
+      return;
+    }
+  }
+  g = 3.0e38f;
+  sd = 3.0e38f;
 }
+
+template <class Src>
+__device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int b, int kind_x, int i, int j) {
+  unsigned int k = atomicAdd(s.count, 1u);
+  if (k < s.cap) {
+    s.items[k] = make_int4(b, kind_x, i, j);
+  } else {
+    s.overflow[src.overflow_slot(b)] = 1;
+  }
+}
+
+struct Smem {
+  double* qbuf;  // generated configurations (edges)
+  float* pose;   // [cfg][slot][12]
+  SphereF* sph;
+  GroupF* grp;
+  PrimF* prm;
+  int2* pairs;
+  int* flags;
+  unsigned* cull;  // [cfg][group]: bit p set -> primitive p certainly clears the whole group
+};
+
+// Where a block's configurations come from and where their outcomes go.
+struct CfgSource {  // a batch of configurations q[B x q_dim]
+  const double* q;
+  int64_t B;
+  uint8_t* out;
+  __device__ int64_t count() const { return B; }
+  __device__ const double* cfg(const PmTablesHdr* T, int64_t i, double*) const { return q + i * T->q_dim; }
+  __device__ bool pre_skip(int64_t) const { return false; }     // before the fast pass: nothing known
+  __device__ bool skip(int64_t i) const { return out[i] == 0; }  // after it: already invalid
+  __device__ void fail(int64_t i) const { out[i] = 0; }
+  __device__ void done(int64_t i, bool failed) const { out[i] = failed ? 0 : 1; }
+  __device__ int64_t overflow_slot(int64_t i) const { return i; }
+  __device__ int64_t n_overflow_slots() const { return B; }
+  __device__ void full_check(const TView& v, const double* state, int64_t i, double*) const {
+    out[i] = is_valid_cfg(v, state, q + i * v.T->q_dim) ? 1 : 0;
+  }
+};
+
+// Edges of checkMotion flattened into waypoints: edge e owns waypoints [off[e], off[e] + n[e]);
+// waypoint k of an edge is s2 for k = 0, then the interior points in the reference's visiting
+// order (motion_validator.cpp:45-78).
+struct EdgeSource {
+  const double* s1;
+  const double* s2;
+  const int64_t* off;
+  const int32_t* n;
+  const double* sr;
+  const int16_t* seq;
+  int64_t E;
+  uint8_t* valid;  // per edge, 1 until a waypoint is found colliding
+  __device__ int64_t edge_of(int64_t w) const {
+    int64_t lo = 0, hi = E - 1;
+    while (lo < hi) {
+      int64_t mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+  }
+  __device__ const double* cfg(const PmTablesHdr* T, int64_t w, double* buf) const {
+    const int64_t e = edge_of(w);
+    const int64_t k = w - off[e];
+    const int d = T->q_dim;
+    const double* a = s1 + e * d;
+    const double* b = s2 + e * d;
+    if (k == 0) return b;
+    const double r = sr[e];
+    const unsigned long long n_test = (unsigned long long)(floor(1 / r) + 2);
+    double t;
+    if (n_test < 129) {
+      t = (double)seq[(n_test - 1) * 128 + (k + 1)] * r;
+    } else {
+      t = (double)k * r;
+    }
+    for (int i = 0; i < d; i++) buf[i] = a[i] + (b[i] - a[i]) * t;
+    return buf;
+  }
+  __device__ bool pre_skip(int64_t w) const { return valid[edge_of(w)] == 0; }
+  __device__ bool skip(int64_t w) const { return valid[edge_of(w)] == 0; }
+  __device__ void fail(int64_t w) const { valid[edge_of(w)] = 0; }
+  __device__ void done(int64_t w, bool failed) const {
+    if (failed) valid[edge_of(w)] = 0;
+  }
+  __device__ int64_t overflow_slot(int64_t w) const { return edge_of(w); }
+  __device__ int64_t n_overflow_slots() const { return E; }
+  // every waypoint of edge e in the plain FP64 method
+  __device__ void full_check(const TView& v, const double* state, int64_t e, double* buf) const {
+    bool ok = true;
+    for (int64_t w = off[e]; w < off[e] + n[e] && ok; w++) ok = is_valid_cfg(v, state, cfg(v.T, w, buf));
+    if (!ok) valid[e] = 0;
+  }
+};
+
+// Phases 1-3 for the configurations [c0, c0 + ncfg) of a source.  qbuf holds CPB * q_dim
+// doubles of shared memory for generated configurations.
+template <int CPB, class Src>
+__device__ void fast_block(const TView& v, const Smem& sm, const double* __restrict__ state, const Src& src, int64_t c0, int ncfg,
+                           float* __restrict__ dist32, float cutoff, const Scratch& scr, double* qbuf) {
+  const PmTablesHdr* T = v.T;
+  const int ns = T->n_spheres, ng = T->n_groups, np = T->n_prims, npr = T->n_pairs, nsl = T->n_slots;
+  const int tid = threadIdx.x;
+  if (tid < CPB) sm.flags[tid] = 0;
+  // ---- 1. FK (FP64, exact) -> FP32 poses
+  if (tid < ncfg) {
+    if (src.pre_skip(c0 + tid)) {
+      sm.flags[tid] = FLAG_FAIL | 2;  // already known invalid: no work
+    } else {
+      DPose pose[PM_MAX_SLOTS];
+      const double* qc = src.cfg(T, c0 + tid, qbuf + tid * T->q_dim);
+      fk64(T, state, qc, T->base_type == PM_BASE_FIXED, pose);
+      float* o = sm.pose + (size_t)tid * nsl * 12;
+      for (int i = 0; i < nsl; i++) {
+        DM3 R = qmat(pose[i].q);
+        for (int k = 0; k < 9; k++) o[12 * i + k] = (float)R.m[k];
+        o[12 * i + 9] = (float)pose[i].t.x;
+        o[12 * i + 10] = (float)pose[i].t.y;
+        o[12 * i + 11] = (float)pose[i].t.z;
+      }
+    }
+  }
+  __syncthreads();
+  const bool want_dist = dist32 != nullptr;
+  // ---- 2. group culling against each primitive
+  for (int t = tid; t < ncfg * ng; t += blockDim.x) {
+    const int c = t / ng, gi = t - c * ng;
+    if (sm.flags[c] & 2) continue;
+    const GroupF& G = sm.grp[gi];
+    const float* P = sm.pose + ((size_t)c * nsl + G.slot) * 12;
+    float3 gc = xf(P, G.rel[0], G.rel[1], G.rel[2]);
+    unsigned mask = 0;
+    const int npc = np < 32 ? np : 32;
+    for (int p = 0; p < npc; p++) {
+      float g, sd, mag;
+      const float extra = margin32(4.0f + fabsf(gc.x) + fabsf(gc.y) + fabsf(gc.z)) + (want_dist ? cutoff : 0.f);
+      clearance(sm.prm[p], v.C, gc.x, gc.y, gc.z, G.radius, G.tiny, extra, g, sd, mag);
+      if (g > margin32(mag) + (want_dist ? cutoff : 0.f)) mask |= 1u << p;
+    }
+    sm.cull[c * ng + gi] = mask;
+  }
+  __syncthreads();
+  // ---- 3. sphere tasks and self-pair tasks
+  const int n_sph_tasks = ncfg * ns;
+  const int n_tasks = n_sph_tasks + ncfg * npr;
+  for (int t = tid; t < n_tasks; t += blockDim.x) {
+    if (t < n_sph_tasks) {
+      const int c = t / ns, si = t - c * ns;
+      if (sm.flags[c] & 2) continue;
+      const SphereF S = sm.sph[si];
+      const GroupF& G = sm.grp[S.group];
+      const bool check = !G.only_self && np > 0;
+      if (!want_dist && (!check || (sm.flags[c] & FLAG_FAIL))) continue;
+      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * 12;
+      const float3 sc = xf(P, S.x, S.y, S.z);
+      const unsigned cm = sm.cull[c * ng + S.group];
+      float sdmin = cutoff;
+      int fail = 0;
+      for (int p = 0; p < np; p++) {
+        if (p < 32 && ((cm >> p) & 1u)) continue;
+        float g, sd, mag;
+        const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z));
+        clearance(sm.prm[p], v.C, sc.x, sc.y, sc.z, S.r, S.tiny, want_dist ? m + cutoff : m, g, sd, mag);
+        sdmin = fminf(sdmin, sd);
+        if (!check) continue;
+        const float mm = margin32(mag);
+        if (g < -mm) {
+          fail = 1;
+          if (!want_dist) break;
+        } else if (g <= mm) {
+          push_item(scr, src, (int)(c0 + c), p << 1, si, 0);
+        }
+      }
+      if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
+      if (want_dist) dist32[(c0 + c) * ns + si] = sdmin;
+    } else {
+      const int u = t - n_sph_tasks;
+      const int c = u / npr, pi = u - c * npr;
+      if (sm.flags[c] & (FLAG_FAIL | 2)) continue;
+      const int2 pr = sm.pairs[pi];
+      const GroupF& G1 = sm.grp[pr.x];
+      const GroupF& G2 = sm.grp[pr.y];
+      const float* P1 = sm.pose + ((size_t)c * nsl + G1.slot) * 12;
+      const float* P2 = sm.pose + ((size_t)c * nsl + G2.slot) * 12;
+      const float3 a = xf(P1, G1.rel[0], G1.rel[1], G1.rel[2]);
+      const float3 bb = xf(P2, G2.rel[0], G2.rel[1], G2.rel[2]);
+      const float ddx = a.x - bb.x, ddy = a.y - bb.y, ddz = a.z - bb.z;
+      const float gmag = fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(bb.x) + fabsf(bb.y) + fabsf(bb.z);
+      if (sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz))) - (G1.radius + G2.radius) > 2.0f * margin32(gmag)) continue;
+      int fail = 0;
+      for (int i = G1.begin; i < G1.begin + G1.count && !fail; i++) {
+        const SphereF Si = sm.sph[i];
+        const float3 ci = xf(P1, Si.x, Si.y, Si.z);
+        for (int j = G2.begin; j < G2.begin + G2.count; j++) {
+          const SphereF Sj = sm.sph[j];
+          const float3 cj = xf(P2, Sj.x, Sj.y, Sj.z);
+          const float ex = ci.x - cj.x, ey = ci.y - cj.y, ez = ci.z - cj.z;
+          const float g = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))) - (Si.r + Sj.r);
+          const float mm = 2.0f * margin32(fabsf(ci.x) + fabsf(ci.y) + fabsf(ci.z) + fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z));
+          if (g < -mm) {
+            fail = 1;
+            break;
+          }
+          if (g <= mm) push_item(scr, src, (int)(c0 + c), (pi << 1) | 1, i, j);
+        }
+      }
+      if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
+    }
+  }
+  __syncthreads();
+  if (tid < ncfg && !(sm.flags[tid] & 2)) src.done(c0 + tid, (sm.flags[tid] & FLAG_FAIL) != 0);
+  __syncthreads();
+}
+
+__device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
+  Smem sm;
+  sm.pose = reinterpret_cast<float*>(p);
+  p += sizeof(float) * 12 * cpb * T->n_slots;
+  sm.sph = reinterpret_cast<SphereF*>(p);
+  p += sizeof(SphereF) * T->n_spheres;
+  sm.grp = reinterpret_cast<GroupF*>(p);
+  p += sizeof(GroupF) * T->n_groups;
+  sm.prm = reinterpret_cast<PrimF*>(p);
+  p += sizeof(PrimF) * T->n_prims;
+  sm.pairs = reinterpret_cast<int2*>(p);
+  p += sizeof(int2) * T->n_pairs;
+  sm.flags = reinterpret_cast<int*>(p);
+  p += sizeof(int) * cpb;
+  sm.cull = reinterpret_cast<unsigned*>(p);
+  p += sizeof(unsigned) * cpb * T->n_groups;
+  p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+  sm.qbuf = reinterpret_cast<double*>(p);
+  return sm;
+}
+
+__device__ void stage_tables(const TView& v, const Smem& sm) {
+  const PmTablesHdr* T = v.T;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < T->n_spheres; i += blockDim.x) {
+    SphereF s;
+    s.x = (float)v.sx[i];
+    s.y = (float)v.sy[i];
+    s.z = (float)v.sz[i];
+    s.r = (float)v.sr[i];
+    s.group = v.sgroup[i];
+    s.tiny = v.sr[i] < 1e-6;
+    sm.sph[i] = s;
+  }
+  for (int i = tid; i < T->n_groups; i += blockDim.x) {
+    const PmGroup& G = v.G[i];
+    GroupF g;
+    g.rel[0] = (float)G.rel[0];
+    g.rel[1] = (float)G.rel[1];
+    g.rel[2] = (float)G.rel[2];
+    g.radius = (float)G.radius;
+    g.slot = G.slot;
+    g.begin = G.begin;
+    g.count = G.count;
+    g.only_self = G.only_self;
+    g.tiny = G.radius < 1e-6;
+    sm.grp[i] = g;
+  }
+  for (int i = tid; i < T->n_prims; i += blockDim.x) {
+    const PmPrim& P = v.P[i];
+    PrimF f;
+    f.kind = P.kind;
+    f.aa = P.axis_aligned;
+    f.za = P.z_axis_aligned;
+    f.cloud = P.cloud;
+    for (int k = 0; k < 3; k++) {
+      f.lb[k] = (float)P.lb[k];
+      f.ub[k] = (float)P.ub[k];
+      f.pos[k] = (float)P.pos[k];
+    }
+    for (int k = 0; k < 9; k++) f.rot[k] = (float)P.rot[k];
+    f.a = (float)P.a;
+    f.b = (float)P.b;
+    f.c = (float)P.c;
+    f.mag = (P.kind == PM_SDF_GROUND || P.kind == PM_SDF_CLOUD)
+                ? (float)fabs(P.a)
+                : (float)(fabs(P.pos[0]) + fabs(P.pos[1]) + fabs(P.pos[2]) + fabs(P.a) + fabs(P.b) + fabs(P.c));
+    sm.prm[i] = f;
+  }
+  for (int i = tid; i < T->n_pairs; i += blockDim.x) sm.pairs[i] = make_int2(v.pairs[2 * i], v.pairs[2 * i + 1]);
+  __syncthreads();
+}
+
+template <int CPB>
+__global__ void __launch_bounds__(128) k_fast_valid(const PmTablesHdr* __restrict__ T, const double* __restrict__ state,
+                                                    const double* __restrict__ q, int64_t B, uint8_t* __restrict__ out,
+                                                    float* __restrict__ dist32, float cutoff, Scratch scr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TView v(T);
+  Smem sm = carve(smem_raw, T, CPB);
+  stage_tables(v, sm);
+  CfgSource src{q, B, out};
+  const int64_t c0 = (int64_t)blockIdx.x * CPB;
+  fast_block<CPB>(v, sm, state, src, c0, (int)(B - c0 < CPB ? B - c0 : CPB), dist32, cutoff, scr, sm.qbuf);
+}
+
+// Persistent work-queue kernel over the flattened waypoints of all edges.
+template <int CPB>
+__global__ void __launch_bounds__(128) k_fast_edges(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, EdgeSource src,
+                                                    unsigned long long* next, Scratch scr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long chunk;
+  TView v(T);
+  Smem sm = carve(smem_raw, T, CPB);
+  stage_tables(v, sm);
+  const int64_t W = src.E > 0 ? src.off[src.E - 1] + src.n[src.E - 1] : 0;
+  for (;;) {
+    if (threadIdx.x == 0) chunk = (long long)atomicAdd(next, (unsigned long long)CPB);
+    __syncthreads();
+    const int64_t c0 = chunk;
+    if (c0 >= W) break;
+    fast_block<CPB>(v, sm, state, src, c0, (int)(W - c0 < CPB ? W - c0 : CPB), nullptr, 0.f, scr, sm.qbuf);
+  }
+}
+
+// Exact FP64 evaluation of the queued terms, and full plain checks of the configurations (or
+// edges) whose terms overflowed the queue.
+template <class Src>
+__global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, Src src, Scratch scr) {
+  TView v(T);
+  const unsigned int n_items = min(*scr.count, scr.cap);
+  const int64_t total = (int64_t)n_items + src.n_overflow_slots();
+  double qbuf[PM_MAX_SLOTS + 8];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < n_items) {
+      const int4 it = scr.items[i];
+      if (src.skip(it.x)) continue;
+      DPose pose[PM_MAX_SLOTS];
+      fk64(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, pose);
+      bool hit = false;
+      if ((it.y & 1) == 0) {  // sphere it.z vs primitive it.y >> 1: gate AND test
+        const PmPrim& P = v.P[it.y >> 1];
+        const PmGroup& g = v.G[v.sgroup[it.z]];
+        const DM3 R = qmat(pose[g.slot].q);
+        const D3 gc = add(mv(R, D3{g.rel[0], g.rel[1], g.rel[2]}), pose[g.slot].t);
+        if (!outside_aabb(P, gc, g.radius) && !prim_outside(P, v.C, gc, g.radius)) {
+          const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
+          hit = !outside_aabb(P, c, v.sr[it.z]) && !prim_outside(P, v.C, c, v.sr[it.z]);
+        }
+      } else {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test
+        const int pr = it.y >> 1;
+        const PmGroup& g1 = v.G[v.pairs[2 * pr]];
+        const PmGroup& g2 = v.G[v.pairs[2 * pr + 1]];
+        const DM3 R1 = qmat(pose[g1.slot].q), R2 = qmat(pose[g2.slot].q);
+        const D3 c1 = add(mv(R1, D3{g1.rel[0], g1.rel[1], g1.rel[2]}), pose[g1.slot].t);
+        const D3 c2 = add(mv(R2, D3{g2.rel[0], g2.rel[1], g2.rel[2]}), pose[g2.slot].t);
+        const double osq = sqn(sub(c1, c2));
+        const double ors = g1.radius + g2.radius;
+        if (!(osq > ors * ors)) {
+          const D3 a = add(mv(R1, v.rel(it.z)), pose[g1.slot].t);
+          const D3 bb = add(mv(R2, v.rel(it.w)), pose[g2.slot].t);
+          const double rs = v.sr[it.z] + v.sr[it.w];
+          hit = sqn(sub(a, bb)) < rs * rs;
+        }
+      }
+      if (hit) src.fail(it.x);
+    } else {
+      const int64_t k = i - n_items;
+      if (!scr.overflow[k]) continue;
+      src.full_check(v, state, k, qbuf);
+      atomicAdd(scr.stats + 2, 1ull);
+    }
+  }
+}
+
+// checkMotion setup: step ratio and number of checked waypoints per edge
+// (motion_validator.cpp:17-79, 89-126): n = 0 when the ratio is infinite, else floor(1/r) + 1.
+__global__ void k_edge_setup(const double* __restrict__ s1, const double* __restrict__ s2, int64_t E, int dim, int type,
+                             const double* __restrict__ width, double resolution, double* __restrict__ sr, int32_t* __restrict__ n,
+                             uint8_t* __restrict__ valid) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const double* a = s1 + e * dim;
+  const double* b = s2 + e * dim;
+  double r;
+  if (type == 0) {
+    double diff_long = 0.0, max_diff = -INFINITY;
+    int li = 0;
+    for (int i = 0; i < dim; i++) {
+      double diff = b[i] - a[i];
+      double asd = fabs(diff) * (1.0 / width[i]);
+      if (asd > max_diff) {
+        max_diff = asd;
+        li = i;
+        diff_long = diff;
+      }
+    }
+    r = fabs(diff_long) < 1e-6 ? INFINITY : width[li] / fabs(diff_long);
+  } else {
+    double dist = 0.0;
+    for (int i = 0; i < dim; i++) {
+      double d = a[i] - b[i];
+      dist += d * d;
+    }
+    r = resolution / sqrt(dist);
+  }
+  sr[e] = r;
+  valid[e] = 1;
+  if (r == INFINITY) {
+    n[e] = 0;
+  } else if (!(r > 0.0) || 1.0 / r > 67108864.0) {  // same bound as the plain kernel
+    n[e] = 0;
+    valid[e] = 0;
+  } else {
+    n[e] = (int32_t)(floor(1 / r) + 1);
+  }
+}
+
+// exclusive scan of n[E] into off[E] with one block (E is at most a few million)
+__global__ void k_scan1(const int32_t* __restrict__ n, int64_t E, int64_t* __restrict__ off) {
+  __shared__ int64_t part[1024];
+  const int tid = threadIdx.x;
+  const int64_t per = (E + blockDim.x - 1) / blockDim.x;
+  const int64_t b = tid * per, e = min(E, b + per);
+  int64_t s = 0;
+  for (int64_t i = b; i < e; i++) s += n[i];
+  part[tid] = s;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    int64_t t = tid >= o ? part[tid - o] : 0;
+    __syncthreads();
+    part[tid] += t;
+    __syncthreads();
+  }
+  int64_t run = part[tid] - s;
+  for (int64_t i = b; i < e; i++) {
+    off[i] = run;
+    run += n[i];
+  }
+}
+
+}  // namespace
+
+namespace pmg {
+
+size_t fast_smem_bytes(const PmTablesHdr& h, int cpb) {
+  return sizeof(float) * 12 * (size_t)cpb * h.n_slots + sizeof(SphereF) * h.n_spheres + sizeof(GroupF) * h.n_groups +
+         sizeof(PrimF) * h.n_prims + sizeof(int2) * h.n_pairs + sizeof(int) * cpb + sizeof(unsigned) * (size_t)cpb * h.n_groups + 16 +
+         sizeof(double) * (size_t)cpb * h.q_dim;
+}
+
+template <class K>
+static cudaError_t prep(K kern, size_t sm) {
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+}
+
+// count, overflow and stats must be zeroed by the caller
+cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
+                              uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
+                              uint8_t* overflow, unsigned long long* stats, int cpb, cudaStream_t s) {
+  if (B <= 0) return cudaSuccess;
+  Scratch scr{items, count, cap, overflow, stats};
+  size_t sm = fast_smem_bytes(h, cpb);
+  if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
+  unsigned grid = (unsigned)((B + cpb - 1) / cpb);
+  cudaError_t e;
+  switch (cpb) {
+    case 16:
+      if ((e = prep(k_fast_valid<16>, sm)) != cudaSuccess) return e;
+      k_fast_valid<16><<<grid, 128, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);
+      break;
+    case 64:
+      if ((e = prep(k_fast_valid<64>, sm)) != cudaSuccess) return e;
+      k_fast_valid<64><<<grid, 128, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);
+      break;
+    default:
+      if ((e = prep(k_fast_valid<32>, sm)) != cudaSuccess) return e;
+      k_fast_valid<32><<<grid, 128, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);
+      break;
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  CfgSource src{q, B, out};
+  k_fast_recheck<CfgSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
+  return cudaGetLastError();
+}
+
+// work: sr (E doubles), n (E int32), off (E int64), next (1 ull), all device; count/overflow(E)/
+// stats/next zeroed by the caller.  out receives the edge booleans.
+cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
+                              int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,
+                              int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
+                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int n_sm, cudaStream_t s) {
+  if (E <= 0) return cudaSuccess;
+  Scratch scr{items, count, cap, overflow, stats};
+  k_edge_setup<<<(unsigned)((E + 127) / 128), 128, 0, s>>>(s1, s2, E, h.q_dim, type, width, resolution, sr, n, out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_scan1<<<1, 1024, 0, s>>>(n, E, off);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  EdgeSource src{s1, s2, off, n, sr, seq, E, out};
+  size_t sm = fast_smem_bytes(h, cpb);
+  if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
+  int per_sm = 0;
+  if ((e = prep(k_fast_edges<32>, sm)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<32>, 128, sm)) != cudaSuccess) return e;
+  unsigned grid = (unsigned)(n_sm * (per_sm > 0 ? per_sm : 1));
+  k_fast_edges<32><<<grid, 128, sm, s>>>(T, state, src, next, scr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  k_fast_recheck<EdgeSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
+  return cudaGetLastError();
+}
+
+}  // namespace pmg

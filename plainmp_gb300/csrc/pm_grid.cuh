@@ -115,8 +115,10 @@ __device__ __forceinline__ float box_d2_32(const float* b, float qx, float qy, f
   float gx = gap32(qx, b[0], b[3]), gy = gap32(qy, b[1], b[4]), gz = gap32(qz, b[2], b[5]);
   return fmaf(gx, gx, fmaf(gy, gy, gz * gz));
 }
-__device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float qy, float qz) {
-  NNResult32 r{INFINITY, -1};
+// maxd2 bounds the search: points at squared distance >= maxd2 are never reported (idx stays -1
+// when none is closer).
+__device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2 = INFINITY) {
+  NNResult32 r{maxd2, -1};
   if (G.n_points <= 0) return r;
   const float inv = (float)(1.0 / G.block);
   const float ox = (float)G.origin[0], oy = (float)G.origin[1], oz = (float)G.origin[2];

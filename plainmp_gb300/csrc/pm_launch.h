@@ -32,6 +32,17 @@ cudaError_t launch_check_motion64(const PmTablesHdr* T, const double* state, con
                                   int type, const double* width, double resolution, const int16_t* seq, uint8_t* out,
                                   unsigned long long* n_checked, cudaStream_t s);
 
+// ---- fast path (k_fast.cu): FP32 decisions + FP64 recheck of uncertain terms.
+size_t fast_smem_bytes(const PmTablesHdr& h, int cpb);
+cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
+                              uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
+                              uint8_t* overflow, unsigned long long* stats, int cpb, cudaStream_t s);
+
+cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
+                              int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,
+                              int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
+                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int n_sm, cudaStream_t s);
+
 // ---- SDF utilities (k_plain.cu): prims/clouds describe one SDF (a union is flattened)
 cudaError_t launch_sdf_points(const PmPrim* prims, int n_prims, const PmGridDev* clouds, int is_union, const double* pts,
                               const double* radii, int64_t n, double* eval_out, uint8_t* outside_out, cudaStream_t s);

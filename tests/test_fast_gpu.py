@@ -1,0 +1,140 @@
+"""GPU parity of the FP32 + FP64-recheck fast paths against the oracle (validity identical to
+the reference; FP32 per-sphere distances within the stated bound)."""
+import numpy as np
+import pytest
+
+from plainmp_gb300 import BoxMotionValidator, EuclideanMotionValidator, Pose, SphereSDF, UnionSDF, scenes
+from plainmp_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+CUTOFF = 0.1
+# FP32 distance error bound: 1e-6 + 64 * 2^-24 * (1 + magnitudes), magnitudes below ~20 m here
+DIST_TOL = 1e-6 + 64 * 2.0 ** -24 * 21
+
+
+@pytest.fixture(scope="module")
+def chain(oracle):
+    r, s = W.chain7_robot(), W.chain7_scene()
+    return scenes.make_constraint(r, s), oracle.make_constraint(r, s)
+
+
+@pytest.fixture(scope="module")
+def dual(oracle):
+    r, s = W.dualarm_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0)
+    return scenes.make_constraint(r, s), oracle.make_constraint(r, s)
+
+
+def test_fast_chain7_matches_oracle(chain):
+    (_, cst, _), (_, oc, _) = chain
+    Q = W.chain7_configs(4096)
+    got, st = cst.is_valid_fast(Q, stats=True)
+    assert np.array_equal(got, oc.is_valid(Q, threads=8))
+    assert np.array_equal(got, cst.is_valid_batch(Q))
+    assert st["configs"] == 4096
+    assert st["rechecked_terms"] < 4096  # a small fraction of the 56 x 20 + 960 terms per config
+
+
+@pytest.mark.parametrize("B", [1, 5, 31, 32, 33, 100])
+def test_fast_ragged(chain, B):
+    (_, cst, _), (_, oc, _) = chain
+    Q = W.chain7_configs(B, seed=17)
+    assert np.array_equal(cst.is_valid_fast(Q), oc.is_valid(Q))
+
+
+def test_fast_chain7_distances(chain):
+    (_, cst, _), (_, oc, _) = chain
+    Q = W.chain7_configs(512, seed=12)
+    ok, d32 = cst.is_valid_fast(Q, distances=True)
+    ref = np.minimum(oc.sphere_distances(Q, threads=8), CUTOFF)
+    assert d32.dtype == np.float32 and d32.shape == (512, 56)
+    assert np.abs(d32.astype(np.float64) - ref).max() < DIST_TOL
+    assert np.array_equal(ok, oc.is_valid(Q, threads=8))
+
+
+def test_fast_dualarm_cloud(dual):
+    (_, cst, _), (_, oc, _) = dual
+    Q = W.dualarm_configs(4096, seed=6)
+    got = cst.is_valid_fast(Q)
+    assert np.array_equal(got, oc.is_valid(Q, threads=8))
+    assert np.array_equal(got, cst.is_valid_batch(Q))
+
+
+def test_fast_dualarm_cloud_distances(dual):
+    (_, cst, _), (_, oc, _) = dual
+    Q = W.dualarm_configs(8, seed=7)
+    ok, d32 = cst.is_valid_fast(Q, distances=True)
+    ref = np.minimum(cst.sphere_distances(Q), CUTOFF)  # plain FP64 grid, exact vs the KD-tree (tested elsewhere)
+    assert np.abs(d32.astype(np.float64) - ref).max() < DIST_TOL
+    assert np.array_equal(ok, oc.is_valid(Q))
+
+
+def test_fast_near_boundary_rechecks(oracle):
+    """Obstacle spheres placed within 1e-15..1e-9 of tangency to one robot sphere per
+    configuration: every such decision is left to the FP64 recheck, which must reproduce the
+    reference bit for bit."""
+    robot = W.chain7_robot()
+    Q = W.chain7_configs(64, seed=31)
+    _, oc0, _ = oracle.make_constraint(robot, None, self_collision=False)
+    _, cen = oc0.sphere_distances(Q, centres=True)
+    order = oc0.groups()["radii"]
+    rng = np.random.default_rng(0)
+    obstacles = []
+    prims = []
+    for b in range(64):
+        s = int(rng.integers(0, 56))
+        c = cen[b, s]
+        direction = rng.standard_normal(3)
+        direction /= np.linalg.norm(direction)
+        R = 0.05 + 0.1 * rng.random()
+        delta = [1e-9, -1e-9, 1e-12, -1e-12, 0.0][b % 5]
+        pos = c + direction * (R + order[s] + delta)
+        obstacles.append(SphereSDF(R, Pose(pos, np.eye(3))))
+        prims.append(W.Primitive("sphere", pos, np.eye(3), (R,)))
+    scene = W.Scene(prims)
+    kin, cst, _ = scenes.make_constraint(robot, None, self_collision=False)
+    cst.set_sdf(UnionSDF(obstacles))
+    _, oc, _ = oracle.make_constraint(robot, scene, self_collision=False)
+    got, st = cst.is_valid_fast(Q, stats=True)
+    ref = oc.is_valid(Q)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(cst.is_valid_batch(Q), ref)
+    # the tangent terms of configurations without a certain collision went through FP64
+    assert st["rechecked_terms"] >= 10
+
+
+def test_fast_mobile_base(oracle):
+    r = W.chain7_robot()
+    r = W.Robot(r.urdf, r.control_joints, r.end_link, r.spheres, r.self_pairs, base_type="PLANAR")
+    s = W.chain7_scene()
+    (_, cst, _), (_, oc, _) = scenes.make_constraint(r, s), oracle.make_constraint(r, s)
+    rng = np.random.default_rng(2)
+    Q = np.concatenate([W.chain7_configs(1024, seed=2), rng.normal(0, 0.3, (1024, 3))], axis=1)
+    assert np.array_equal(cst.is_valid_fast(Q), oc.is_valid(Q, threads=8))
+
+
+def test_fast_edges_match_oracle(chain):
+    (_, cst, _), (_, oc, _) = chain
+    s1, s2 = W.chain7_edges(1024)
+    w = np.full(7, 0.05)
+    mv = BoxMotionValidator(cst, w)
+    got, st = mv.check_motion_fast(s1, s2, stats=True)
+    ref, _ = oc.check_motion(s1, s2, 0, w, threads=8)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(got, mv.check_motion_batch(s1, s2))
+    ev = EuclideanMotionValidator(cst, 0.1)
+    got = ev.check_motion_fast(s1[:300], s2[:300])
+    ref, _ = oc.check_motion(s1[:300], s2[:300], 1, None, 0.1, threads=8)
+    assert np.array_equal(got, ref)
+
+
+def test_fast_edges_degenerate(chain):
+    (_, cst, _), (_, oc, _) = chain
+    q = W.chain7_configs(4, seed=40)
+    s1 = np.concatenate([q, q[:2]])
+    s2 = np.concatenate([q + 1e-8, q[2:] + 0.3])  # zero-length edges are valid without a check
+    w = np.full(7, 0.05)
+    got = BoxMotionValidator(cst, w).check_motion_fast(s1, s2)
+    ref, _ = oc.check_motion(s1, s2, 0, w)
+    assert np.array_equal(got, ref)
+    assert got[:4].all()
