@@ -193,6 +193,14 @@ int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t
 int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type,
                             const double* width, double resolution, uint8_t* out, int64_t* stats, int mem, void* stream);
 
+/* ---------------------------------------------------------------- instrumentation
+ * Opt-in timing of the library's own kernels: when enabled, CUDA events are recorded around
+ * every kernel launch on the stream it is launched on.  pmgpu_profile_read synchronises,
+ * returns the summed device time (ms) and launch count of the named kernel since the last
+ * read ("*" = all kernels) and clears them.  No counterpart in the reference. */
+int pmgpu_profile_enable(int on);
+int pmgpu_profile_read(const char* kernel, double* total_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

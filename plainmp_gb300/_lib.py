@@ -101,6 +101,8 @@ _SIGS = {
     "pmgpu_cst_is_valid_fast": (_i, [_p, _p, _i64, _p, _p, _p, _i, _p]),
     "pmgpu_check_motion": (_i, [_p, _p, _p, _i64, _i, _p, _d, _p, _i64p, _i, _p]),
     "pmgpu_check_motion_fast": (_i, [_p, _p, _p, _i64, _i, _p, _d, _p, _p, _i, _p]),
+    "pmgpu_profile_enable": (_i, [_i]),
+    "pmgpu_profile_read": (_i, [C.c_char_p, _dp, _i64p]),
 }
 
 for _name, (_res, _args) in _SIGS.items():
@@ -121,6 +123,19 @@ def check(rc: int) -> None:
     if rc == PMGPU_ERR_TIMEOUT:
         raise DeviceTimeout(msg)
     raise RuntimeError(msg)
+
+
+def profile_enable(on: bool = True) -> None:
+    """Record CUDA events around every library kernel launch (on its own stream)."""
+    check(lib.pmgpu_profile_enable(int(bool(on))))
+
+
+def profile_read(kernel: str = "*"):
+    """(summed device ms, launches) of a library kernel since the last read; clears them."""
+    ms = C.c_double(0.0)
+    n = C.c_int64(0)
+    check(lib.pmgpu_profile_read(kernel.encode(), C.byref(ms), C.byref(n)))
+    return float(ms.value), int(n.value)
 
 
 def device_count() -> int:

@@ -174,12 +174,20 @@ class SphereCollisionCst:
         check(lib.pmgpu_cst_sphere_distances(self._h, b.ptr, b.shape[0], int(bool(high_accuracy)), dptr_, cptr, b.mem, b.stream))
         return (dist, cen) if centres else dist
 
-    def is_valid_fast(self, Q, distances: bool = False, stats: bool = False):
+    def is_valid_fast(self, Q, distances: bool = False, stats: bool = False, out=None, dist_out=None):
         """FP32 + FP64-recheck path: validity identical to is_valid_batch; optional FP32
-        per-sphere distances (B, n_spheres) and recheck statistics."""
+        per-sphere signed distances clamped at the reference's 0.1 m cutoff (B, n_spheres) and
+        recheck statistics.  out / dist_out may be preallocated buffers (e.g. pinned host
+        arrays) in the same memory space as Q."""
         b = self._batch(Q)
-        out, optr = b.empty((b.shape[0],), np.uint8)
-        dist, dp = b.empty((b.shape[0], self.n_spheres), np.float32) if distances else (None, None)
+        if out is not None:
+            optr = Batch(out, np.uint8).ptr
+        else:
+            out, optr = b.empty((b.shape[0],), np.uint8)
+        if distances and dist_out is not None:
+            dist, dp = dist_out, Batch(dist_out, np.float32).ptr
+        else:
+            dist, dp = b.empty((b.shape[0], self.n_spheres), np.float32) if distances else (None, None)
         st = np.zeros(4, dtype=np.int64)
         check(lib.pmgpu_cst_is_valid_fast(self._h, b.ptr, b.shape[0], optr, dp, C.c_void_p(st.ctypes.data) if stats else None,
                                           b.mem, b.stream))

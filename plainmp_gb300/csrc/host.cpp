@@ -70,6 +70,41 @@ static void require_device() {
   }
 }
 
+// ---------------------------------------------------------------------------- kernel timing
+namespace {
+struct ProfRec {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  double total_ms = 0;
+  int64_t launches = 0;
+};
+std::mutex g_prof_mu;
+std::map<std::string, ProfRec> g_prof;
+std::map<std::string, cudaEvent_t> g_prof_open;
+std::atomic<bool> g_prof_enabled{false};
+}  // namespace
+
+bool prof_on() { return g_prof_enabled.load(); }
+void prof_begin(const char* kernel, cudaStream_t s) {
+  if (!prof_on()) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, s);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_open[kernel] = e;
+}
+void prof_end(const char* kernel, cudaStream_t s) {
+  if (!prof_on()) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  auto it = g_prof_open.find(kernel);
+  if (it == g_prof_open.end()) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, s);
+  g_prof[kernel].pending.push_back({it->second, e});
+  g_prof[kernel].launches++;
+  g_prof_open.erase(it);
+}
+
 // ---------------------------------------------------------------------------- device buffers
 struct DevBuf {
   void* p = nullptr;
@@ -1667,6 +1702,35 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
         stats[3] = 0;
       }
     }
+  });
+}
+
+int pmgpu_profile_enable(int on) {
+  return guarded([&] { g_prof_enabled = on != 0; });
+}
+int pmgpu_profile_read(const char* kernel, double* total_ms, int64_t* launches) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    double tot = 0;
+    int64_t n = 0;
+    for (auto& kv : g_prof) {
+      if (kernel && std::strcmp(kernel, "*") != 0 && kv.first != kernel) continue;
+      for (auto& pr : kv.second.pending) {
+        cuda_check(cudaEventSynchronize(pr.second), "profile");
+        float ms = 0;
+        cuda_check(cudaEventElapsedTime(&ms, pr.first, pr.second), "profile");
+        kv.second.total_ms += ms;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+      }
+      kv.second.pending.clear();
+      tot += kv.second.total_ms;
+      n += kv.second.launches;
+      kv.second.total_ms = 0;
+      kv.second.launches = 0;
+    }
+    if (total_ms) *total_ms = tot;
+    if (launches) *launches = n;
   });
 }
 

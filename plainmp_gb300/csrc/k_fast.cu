@@ -593,6 +593,7 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
   cudaError_t e;
+  prof_begin("k_fast_valid", s);
   switch (cpb) {
     case 16:
       if ((e = prep(k_fast_valid<16>, sm)) != cudaSuccess) return e;
@@ -608,8 +609,11 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
       break;
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  prof_end("k_fast_valid", s);
   CfgSource src{q, B, out};
+  prof_begin("k_fast_recheck", s);
   k_fast_recheck<CfgSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
+  prof_end("k_fast_recheck", s);
   return cudaGetLastError();
 }
 
@@ -633,9 +637,13 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if ((e = prep(k_fast_edges<32>, sm)) != cudaSuccess) return e;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<32>, 128, sm)) != cudaSuccess) return e;
   unsigned grid = (unsigned)(n_sm * (per_sm > 0 ? per_sm : 1));
+  prof_begin("k_fast_edges", s);
   k_fast_edges<32><<<grid, 128, sm, s>>>(T, state, src, next, scr);
+  prof_end("k_fast_edges", s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  prof_begin("k_fast_recheck_edges", s);
   k_fast_recheck<EdgeSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
+  prof_end("k_fast_recheck_edges", s);
   return cudaGetLastError();
 }
 

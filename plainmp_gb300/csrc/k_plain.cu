@@ -519,7 +519,9 @@ cudaError_t launch_link_poses(const double* state, const int32_t* parents, const
 cudaError_t launch_is_valid64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, uint8_t* out,
                               cudaStream_t s) {
   if (B <= 0) return cudaSuccess;
+  prof_begin("k_is_valid64", s);
   k_is_valid64<<<grid_for(B, 128), 128, 0, s>>>(T, state, q, B, out);
+  prof_end("k_is_valid64", s);
   return cudaGetLastError();
 }
 cudaError_t launch_evaluate64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int high_accuracy,

@@ -9,6 +9,11 @@
 
 namespace pmg {
 
+// ---- opt-in kernel timing (host.cpp): events around a launch on its stream
+bool prof_on();
+void prof_begin(const char* kernel, cudaStream_t s);
+void prof_end(const char* kernel, cudaStream_t s);
+
 // ---- model state (k_plain.cu)
 // recs: per joint to set, a PmSlot whose `link` is the child link and mode REV/PRIS.
 cudaError_t launch_set_joints(double* state, const PmSlot* recs, const double* q, int n, int accurate, cudaStream_t s);
