@@ -268,8 +268,14 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     const int npc = np < 32 ? np : 32;
     for (int p = 0; p < npc; p++) {
       float g, sd, mag;
-      const float extra = margin32(4.0f + fabsf(gc.x) + fabsf(gc.y) + fabsf(gc.z)) + (want_dist ? cutoff : 0.f);
-      clearance(sm.prm[p], v.C, gc.x, gc.y, gc.z, G.radius, G.tiny, extra, g, sd, mag);
+      const PrimF& P = sm.prm[p];
+      if (P.kind == PM_SDF_CLOUD) {  // the block distance field bounds the cloud from below
+        const float lb = grid_lower_bound32(v.C[P.cloud], gc.x, gc.y, gc.z);
+        g = lb - P.a - G.radius;
+        mag = fabsf(gc.x) + fabsf(gc.y) + fabsf(gc.z) + lb;
+      } else {
+        clearance(P, v.C, gc.x, gc.y, gc.z, G.radius, G.tiny, 0.f, g, sd, mag);
+      }
       if (g > margin32(mag) + (want_dist ? cutoff : 0.f)) mask |= 1u << p;
     }
     sm.cull[c * ng + gi] = mask;

@@ -134,6 +134,42 @@ __global__ void k_block_records(const int32_t* __restrict__ recidx_ex, int64_t n
   }
 }
 
+// Chebyshev (L-infinity) distance transform of the block occupancy, separable: one pass per
+// axis, each line scanned in O(n^2) (n <= a few hundred blocks).
+__global__ void k_edf_pass(const int32_t* __restrict__ blk_occ, const int16_t* __restrict__ in, int16_t* __restrict__ out, int nbx, int nby,
+                           int nbz, int axis) {
+  const int n[3] = {nbx, nby, nbz};
+  const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+  int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= n[a1] * n[a2]) return;
+  int c[3];
+  c[a1] = line % n[a1];
+  c[a2] = line / n[a1];
+  const int len = n[axis];
+  for (int i = 0; i < len; i++) {
+    int best = 32767;
+    for (int j = 0; j < len; j++) {
+      c[axis] = j;
+      const int b = c[0] + nbx * (c[1] + nby * c[2]);
+      int v;
+      if (axis == 0) {
+        v = blk_occ[2 * b] < blk_occ[2 * b + 1] ? 0 : 32767;
+      } else {
+        v = in[b];
+      }
+      if (v == 32767) continue;
+      const int d = max(abs(i - j), v);
+      best = min(best, d);
+    }
+    c[axis] = i;
+    out[c[0] + nbx * (c[1] + nby * c[2])] = (int16_t)best;
+  }
+}
+__global__ void k_edf_final(const int16_t* __restrict__ in, int64_t n, uint8_t* __restrict__ edf) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) edf[i] = (uint8_t)min((int)in[i], 255);
+}
+
 inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -169,6 +205,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   double *px = nullptr, *py = nullptr, *pz = nullptr;
   float4* p32 = nullptr;
   int32_t *blk_occ = nullptr, *cell_pts = nullptr;
+  uint8_t* edf = nullptr;
   float *blk_box = nullptr, *cell_box = nullptr;
   int32_t n_rec = 0;
   do {
@@ -209,6 +246,17 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     k_block_records<<<nblk(nblocks, 128), 128, 0, s>>>(recidx, nblocks, n_rec, cell_box, blk_occ, blk_box);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
+    {
+      int16_t *t0 = nullptr, *t1 = nullptr;
+      if ((e = scratch(nblocks * 2, (void**)&t0)) != cudaSuccess) break;
+      if ((e = scratch(nblocks * 2, (void**)&t1)) != cudaSuccess) break;
+      if ((e = keep(nblocks, (void**)&edf)) != cudaSuccess) break;
+      k_edf_pass<<<nblk((int64_t)nb[1] * nb[2], 64), 64, 0, s>>>(blk_occ, nullptr, t0, nb[0], nb[1], nb[2], 0);
+      k_edf_pass<<<nblk((int64_t)nb[0] * nb[2], 64), 64, 0, s>>>(blk_occ, t0, t1, nb[0], nb[1], nb[2], 1);
+      k_edf_pass<<<nblk((int64_t)nb[0] * nb[1], 64), 64, 0, s>>>(blk_occ, t1, t0, nb[0], nb[1], nb[2], 2);
+      k_edf_final<<<nblk(nblocks, 256), 256, 0, s>>>(t0, nblocks, edf);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+    }
     e = cudaStreamSynchronize(s);
   } while (false);
   for (void* p : tmp) cudaFree(p);
@@ -224,7 +272,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.blk_box = blk_box;
   d.cell_box = cell_box;
   d.cell_pts = cell_pts;
-  d.seed = nullptr;
+  d.edf = edf;
   d.n_points = (int32_t)n;
   return cudaSuccess;
 }

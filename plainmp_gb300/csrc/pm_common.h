@@ -77,7 +77,7 @@ struct PmGridDev {
   const float* blk_box;    // per block: lo xyz, hi xyz (empty: +inf/-inf)
   const float* cell_box;   // per occupied cell: lo xyz, hi xyz
   const int32_t* cell_pts; // per occupied cell: [first point, end)
-  const int32_t* seed;     // per block: index of a point near the block (upper-bound seed)
+  const uint8_t* edf;      // per block: Chebyshev distance in blocks to the nearest occupied block (capped at 255)
   int32_t nbx, nby, nbz;   // blocks per axis
   int32_t n_points;
   double origin[3];        // grid origin (world)

@@ -38,21 +38,30 @@ struct NNResult64 {
   int32_t idx;  // sorted point index, -1 if the cloud is empty
 };
 
-// Exact FP64 nearest squared distance.  The loop over rings is bounded by the grid size.
-__device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q) {
-  NNResult64 r{INFINITY, -1};
+// Exact FP64 nearest squared distance among the points with squared distance below maxd2
+// (idx = -1 when there is none).  The walk starts at the ring of the nearest occupied block
+// (rings inside it hold no point) and is bounded by the grid size.
+__device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q, double maxd2 = INFINITY) {
+  NNResult64 r{maxd2, -1};
   if (G.n_points <= 0) return r;
   const double inv = 1.0 / G.block;
   int cb[3];
   const double qa[3] = {q.x, q.y, q.z};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
+  bool inside = true;
   for (int a = 0; a < 3; a++) {
     double f = floor((qa[a] - G.origin[a]) * inv);
+    if (!(f >= 0 && f <= nb[a] - 1)) inside = false;
     int c = f < 0 ? 0 : (f > nb[a] - 1 ? nb[a] - 1 : (int)f);
     cb[a] = c;
   }
+  const int k0 = G.edf[cb[0] + nb[0] * (cb[1] + nb[1] * cb[2])];
+  if (inside && k0 >= 2) {  // every point lies at least (k0 - 1) blocks away from q's block
+    const double lb0 = (double)(k0 - 1) * G.block - 1e-9;
+    if (lb0 > 0 && lb0 * lb0 >= r.d2) return r;
+  }
   const int kmax = max(nb[0], max(nb[1], nb[2]));
-  for (int K = 0; K <= kmax; K++) {
+  for (int K = min(k0, kmax); K <= kmax; K++) {
     const int z0 = max(cb[2] - K, 0), z1 = min(cb[2] + K, nb[2] - 1);
     const int y0 = max(cb[1] - K, 0), y1 = min(cb[1] + K, nb[1] - 1);
     const int x0 = max(cb[0] - K, 0), x1 = min(cb[0] + K, nb[0] - 1);
@@ -127,12 +136,19 @@ __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float 
   const float oa[3] = {ox, oy, oz};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
   int cb[3];
+  bool inside = true;
   for (int a = 0; a < 3; a++) {
     float f = floorf((qa[a] - oa[a]) * inv);
+    if (!(f >= 0.f && f <= (float)(nb[a] - 1))) inside = false;
     cb[a] = f < 0.f ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
   }
+  const int k0 = __ldg(G.edf + cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]));
+  if (inside && k0 >= 2) {
+    const float lb0 = (float)(k0 - 1) * blk - 4e-6f;
+    if (lb0 > 0.f && lb0 * lb0 >= r.d2) return r;
+  }
   const int kmax = max(nb[0], max(nb[1], nb[2]));
-  for (int K = 0; K <= kmax; K++) {
+  for (int K = min(k0, kmax); K <= kmax; K++) {
     const int z0 = max(cb[2] - K, 0), z1 = min(cb[2] + K, nb[2] - 1);
     const int y0 = max(cb[1] - K, 0), y1 = min(cb[1] + K, nb[1] - 1);
     const int x0 = max(cb[0] - K, 0), x1 = min(cb[0] + K, nb[0] - 1);
@@ -175,6 +191,24 @@ __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float 
     if (lbm > 0.f && lbm * lbm >= r.d2) break;
   }
   return r;
+}
+
+// Lower bound (FP32, conservative by 4 um) on the distance from q to any cloud point, from the
+// block distance field alone: 0 when q is outside the grid or near an occupied block.
+__device__ __forceinline__ float grid_lower_bound32(const PmGridDev& G, float qx, float qy, float qz) {
+  if (G.n_points <= 0) return INFINITY;
+  const float inv = (float)(1.0 / G.block);
+  const float qa[3] = {qx, qy, qz};
+  const float oa[3] = {(float)G.origin[0], (float)G.origin[1], (float)G.origin[2]};
+  const int nb[3] = {G.nbx, G.nby, G.nbz};
+  int cb[3];
+  for (int a = 0; a < 3; a++) {
+    float f = floorf((qa[a] - oa[a]) * inv);
+    if (!(f >= 0.f && f <= (float)(nb[a] - 1))) return 0.f;
+    cb[a] = (int)f;
+  }
+  const int k0 = __ldg(G.edf + cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]));
+  return k0 >= 2 ? fmaxf((float)(k0 - 1) * (float)G.block - 4e-6f, 0.f) : 0.f;
 }
 
 }  // namespace pmd

@@ -18,7 +18,12 @@ __device__ __forceinline__ bool prim_outside(const PmPrim& P, const PmGridDev* c
     case PM_SDF_GROUND:  // primitive_sdf.hpp:246-248
       return p.z + P.a > r;
     case PM_SDF_CLOUD: {  // primitive_sdf.hpp:597-603
-      NNResult64 nn = grid_nearest64(clouds[P.cloud], p);
+      // Only whether some point lies within r + radius matters: search below a reach slightly
+      // beyond it.  A point found there gives the exact KD-tree distance; none found means
+      // sqrt(d2) - radius > r holds with a 1e-12 relative slack, far above rounding.
+      const double reach = (r + P.a) * (1.0 + 1e-12) + 1e-12;
+      NNResult64 nn = grid_nearest64(clouds[P.cloud], p, reach * reach);
+      if (nn.idx < 0) return true;
       return sqrt(nn.d2) - P.a > r;
     }
   }
