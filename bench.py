@@ -216,6 +216,12 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    from plainmp_gb300 import autotune
+
+    shape_dist, _ = autotune.autotune(cst, Q, distances=True)
+    shape_valid, _ = autotune.autotune(cst, Q, distances=False)
+    cst.set_fast_launch(*shape_dist)
+
     def step():
         cst.is_valid_fast(Q, distances=True, out=out, dist_out=dout)
 
@@ -269,7 +275,9 @@ def main():
             tt += start.elapsed_time(end)
         return tt / n
 
+    cst.set_fast_launch(*shape_valid)
     ms_valid = timed(lambda: cst.is_valid_fast(Q, out=out), 5)
+    cst.set_fast_launch(*shape_dist)
     ms_plain = timed(lambda: cst.is_valid_batch(Q), 3)
     ok_fast = cst.is_valid_fast(Q).cpu().numpy()
     ok_plain = cst.is_valid_batch(Q).cpu().numpy()
@@ -320,7 +328,7 @@ def main():
         "vs_baseline": None,
         "dtype": "f32 (FP64 FK and FP64 recheck of uncertain decisions)",
         "data": "synthetic (seeded generators in plainmp_gb300/workloads.py)",
-        "config": config_dict(),
+        "config": config_dict({"launch_shape": {"with_distances": list(shape_dist), "validity_only": list(shape_valid)}}),
         "e2e": {"value": e2e_value, "unit": "configs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": all_n,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

@@ -180,6 +180,12 @@ int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int hig
 int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats,
                             int mem, void* stream);
 
+/* Launch shape of the fast kernel: configurations per block and threads per block, one of
+ * (16,128) (32,128) (32,256) (64,256) (32,512) (64,512) (128,512); chosen per workload by the
+ * autotuner (plainmp_gb300/autotune.py).  No counterpart in the reference. */
+int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block);
+int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* threads_per_block);
+
 /* ---------------------------------------------------------------- motion validator
  * CustomValidatorBase::checkMotion(s1, s2) (ompl/motion_validator.cpp:17-79) for E edges
  * with BoxMotionValidator (type 0, width[q_dim], :89-111) or EuclideanMotionValidator

@@ -101,6 +101,8 @@ _SIGS = {
     "pmgpu_cst_is_valid_fast": (_i, [_p, _p, _i64, _p, _p, _p, _i, _p]),
     "pmgpu_check_motion": (_i, [_p, _p, _p, _i64, _i, _p, _d, _p, _i64p, _i, _p]),
     "pmgpu_check_motion_fast": (_i, [_p, _p, _p, _i64, _i, _p, _d, _p, _p, _i, _p]),
+    "pmgpu_cst_set_fast_launch": (_i, [_p, _i, _i]),
+    "pmgpu_cst_get_fast_launch": (_i, [_p, C.POINTER(_i), C.POINTER(_i)]),
     "pmgpu_profile_enable": (_i, [_i]),
     "pmgpu_profile_read": (_i, [C.c_char_p, _dp, _i64p]),
 }

@@ -174,6 +174,15 @@ class SphereCollisionCst:
         check(lib.pmgpu_cst_sphere_distances(self._h, b.ptr, b.shape[0], int(bool(high_accuracy)), dptr_, cptr, b.mem, b.stream))
         return (dist, cen) if centres else dist
 
+    def set_fast_launch(self, configs_per_block: int, threads_per_block: int) -> None:
+        """Launch shape of the fast kernel (see plainmp_gb300.autotune)."""
+        check(lib.pmgpu_cst_set_fast_launch(self._h, int(configs_per_block), int(threads_per_block)))
+
+    def get_fast_launch(self) -> Tuple[int, int]:
+        a, b = C.c_int(), C.c_int()
+        check(lib.pmgpu_cst_get_fast_launch(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def is_valid_fast(self, Q, distances: bool = False, stats: bool = False, out=None, dist_out=None):
         """FP32 + FP64-recheck path: validity identical to is_valid_batch; optional FP32
         per-sphere signed distances clamped at the reference's 0.1 m cutoff (B, n_spheres) and

@@ -588,6 +588,7 @@ struct HostCst {
   std::vector<std::shared_ptr<HostSdf>> flat;
   PmTablesHdr hdr{};  // host copy of the device table header
   int fast_cpb = 32;  // configurations per block of the fast kernel
+  int fast_nt = 256;  // threads per block of the fast kernel
   std::vector<int> slot_of_link;
   std::vector<PmSlot> ctrl_recs;  // per control joint (child link, REV/PRIS) for state updates
   DevBuf d_ctrl_recs;
@@ -1543,6 +1544,24 @@ int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int hig
     cuda_check(cudaStreamSynchronize(s), "sphere distances");
   });
 }
+int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    static const int ok[][2] = {{16, 128}, {32, 128}, {32, 256}, {64, 256}, {32, 512}, {64, 512}, {128, 512}};
+    bool found = false;
+    for (auto& p : ok) found = found || (p[0] == configs_per_block && p[1] == threads_per_block);
+    if (!found) throw std::invalid_argument("unsupported (configs_per_block, threads_per_block) pair");
+    c->c.fast_cpb = configs_per_block;
+    c->c.fast_nt = threads_per_block;
+  });
+}
+int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* threads_per_block) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    *configs_per_block = c->c.fast_cpb;
+    *threads_per_block = c->c.fast_nt;
+  });
+}
 int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats, int mem,
                             void* stream) {
   return guarded([&] {
@@ -1569,7 +1588,8 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
       dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)B, 16));
       dd = dist32 ? (float*)C.w_out2.ensure(std::max<size_t>((size_t)B * C.n_spheres() * 4, 16)) : nullptr;
     }
-    cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, s), "is_valid_fast");
+    cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s),
+               "is_valid_fast");
     if (mem == PMGPU_MEM_HOST) {
       stage_out(out, dout, (size_t)B, s);
       if (dist32) stage_out(dist32, dd, (size_t)B * C.n_spheres(), s);

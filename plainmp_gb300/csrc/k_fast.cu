@@ -15,6 +15,10 @@
 // [gate(g,p) AND OR_s test(s,p)] = OR over (s,p) of [gate(g(s),p) AND test(s,p)]; a sphere
 // that certainly collides by more than the margin lies inside its group sphere, whose gate then
 // also fails, so certain terms need no FP64 work.  Self pairs factor the same way.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "pm_launch.h"
 #include "pm_view.cuh"
 
@@ -135,6 +139,127 @@ __device__ __forceinline__ void clearance(const PrimF& P, const PmGridDev* cloud
   sd = 3.0e38f;
 }
 
+__device__ __forceinline__ unsigned long long nn_key(float d2, int idx) {
+  return ((unsigned long long)__float_as_uint(d2) << 32) | (unsigned)idx;
+}
+
+// Block offsets (dx, dy, dz) with max |d| <= kOffR, sorted by the minimum distance between two
+// blocks at that offset, sqrt(sum max(|d|-1, 0)^2) block edges (c_off_lb).
+constexpr int kOffR = 6;
+constexpr int kOffN = (2 * kOffR + 1) * (2 * kOffR + 1) * (2 * kOffR + 1);
+__device__ char4 c_off[kOffN];     // global memory: lanes read different entries
+__device__ float c_off_lb[kOffN];
+
+// Warp-cooperative bounded nearest neighbour (FP32): all 32 lanes call it with the same query.
+// Blocks are visited nearest-first, 32 offsets at a time, until the next offset's lower bound
+// clears the current best; every block that may hold a point below the best is handed to all
+// lanes, which split its occupied cells and test their points; the warp minimum is shared after
+// every block.  Result: the exact minimum of the FP32 squared distances below maxd2 (among
+// equal values the smallest sorted index), as grid_nearest32.
+__device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  NNResult32 r{maxd2, -1};
+  if (G.n_points <= 0) return r;
+  float best = maxd2;
+  int bidx = -1;
+  const float reach = sqrtf(maxd2);
+  const float blk = (float)G.block;
+  const float inv = (float)(1.0 / G.block);
+  const float qa[3] = {qx, qy, qz};
+  const float oa[3] = {(float)G.origin[0], (float)G.origin[1], (float)G.origin[2]};
+  const int nb[3] = {G.nbx, G.nby, G.nbz};
+  int cb[3];
+  bool inside = true;
+  for (int a = 0; a < 3; a++) {
+    const float f = floorf((qa[a] - oa[a]) * inv);
+    if (!(f >= 0.f && f <= (float)(nb[a] - 1))) inside = false;
+    cb[a] = f < 0.f ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
+  }
+  auto process = [&](bool cand, int2 occ) {
+    unsigned bal = __ballot_sync(FULL, cand);
+    while (bal) {
+      const int src = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const int c0 = __shfl_sync(FULL, occ.x, src), c1 = __shfl_sync(FULL, occ.y, src);
+      for (int c = c0 + lane; c < c1; c += 32) {
+        if (box_d2_32(G.cell_box + 6 * c, qx, qy, qz) >= best) continue;
+        const int2 pr = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + c);
+        for (int p = pr.x; p < pr.y; p++) {
+          const float4 pt = __ldg(G.p32 + p);
+          const float dx = pt.x - qx, dy = pt.y - qy, dz = pt.z - qz;
+          const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (d2 < best || (d2 == best && bidx >= 0 && p < bidx)) {
+            best = d2;
+            bidx = p;
+          }
+        }
+      }
+      unsigned long long k = nn_key(best, bidx);
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long k2 = __shfl_xor_sync(FULL, k, o);
+        k = k2 < k ? k2 : k;
+      }
+      best = __uint_as_float((unsigned)(k >> 32));
+      bidx = (int)(unsigned)(k & 0xffffffffu);
+    }
+  };
+  if (inside && reach < (float)(kOffR - 1) * blk) {
+    // nearest-first over the sorted offsets; q lies in block cb up to FP32 rounding (4 um slack)
+    for (int base = 0; base < kOffN; base += 32) {
+      if (__ldg(c_off_lb + base) * blk - 4e-6f >= sqrtf(best)) break;
+      const int k = base + lane;
+      bool cand = false;
+      int2 occ = make_int2(0, 0);
+      if (k < kOffN) {
+        const char4 o = __ldg(c_off + k);
+        const int bx = cb[0] + o.x, by = cb[1] + o.y, bz = cb[2] + o.z;
+        if (bx >= 0 && by >= 0 && bz >= 0 && bx < nb[0] && by < nb[1] && bz < nb[2]) {
+          const int b = bx + nb[0] * (by + nb[1] * bz);
+          occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + b);
+          cand = occ.x < occ.y && box_d2_32(G.blk_box + 6 * b, qx, qy, qz) < best;
+        }
+      }
+      process(cand, occ);
+    }
+  } else {
+    // the cube of blocks [q - reach, q + reach]
+    int lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+      // 1e-3 block of slack covers the FP32 rounding of the range against the FP64 assignment
+      const float f0 = floorf((qa[a] - reach - oa[a]) * inv - 1e-3f), f1 = floorf((qa[a] + reach - oa[a]) * inv + 1e-3f);
+      if (f1 < 0.f || f0 > (float)(nb[a] - 1)) return r;
+      lo[a] = f0 < 0.f ? 0 : (int)f0;
+      hi[a] = f1 > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f1;
+    }
+    const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const int nblk = nx * ny * nz;
+    for (int base = 0; base < nblk; base += 32) {
+      const int i = base + lane;
+      bool cand = false;
+      int2 occ = make_int2(0, 0);
+      if (i < nblk) {
+        const int bx = lo[0] + i % nx;
+        const int t = i / nx;
+        const int by = lo[1] + t % ny, bz = lo[2] + t / ny;
+        const int b = bx + nb[0] * (by + nb[1] * bz);
+        occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + b);
+        cand = occ.x < occ.y && box_d2_32(G.blk_box + 6 * b, qx, qy, qz) < best;
+      }
+      process(cand, occ);
+    }
+  }
+  r.d2 = best;
+  r.idx = bidx;
+  return r;
+}
+
+__device__ __forceinline__ int f2o(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
 template <class Src>
 __device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int b, int kind_x, int i, int j) {
   unsigned int k = atomicAdd(s.count, 1u);
@@ -147,6 +272,9 @@ __device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int 
 
 struct Smem {
   double* qbuf;  // generated configurations (edges)
+  int2* hq;      // hard cloud queries: (cfg * n_spheres + sphere, primitive)
+  int* hq_n;     // [0] pushed, [1] popped
+  int* sdist;    // per (cfg, sphere): running minimum signed distance, order-preserving int
   float* pose;   // [cfg][slot][12]
   SphereF* sph;
   GroupF* grp;
@@ -281,7 +409,14 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     sm.cull[c * ng + gi] = mask;
   }
   __syncthreads();
-  // ---- 3. sphere tasks and self-pair tasks
+  // ---- 3a. sphere tasks (primitives in-thread; cloud queries near the cloud are queued) and
+  //          self-pair tasks
+  if (tid == 0) {
+    sm.hq_n[0] = 0;
+    sm.hq_n[1] = 0;
+  }
+  __syncthreads();
+  const int hq_cap = T->n_clouds > 0 ? CPB * ns : 0;
   const int n_sph_tasks = ncfg * ns;
   const int n_tasks = n_sph_tasks + ncfg * npr;
   for (int t = tid; t < n_tasks; t += blockDim.x) {
@@ -297,11 +432,23 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       const unsigned cm = sm.cull[c * ng + S.group];
       float sdmin = cutoff;
       int fail = 0;
+      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z));
       for (int p = 0; p < np; p++) {
         if (p < 32 && ((cm >> p) & 1u)) continue;
+        const PrimF& Pr = sm.prm[p];
         float g, sd, mag;
-        const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z));
-        clearance(sm.prm[p], v.C, sc.x, sc.y, sc.z, S.r, S.tiny, want_dist ? m + cutoff : m, g, sd, mag);
+        if (Pr.kind == PM_SDF_CLOUD) {
+          const float lb = grid_cell_lower_bound32(v.C[Pr.cloud], sc.x, sc.y, sc.z);
+          if (lb - Pr.a - S.r > margin32(fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z) + lb) + (want_dist ? cutoff : 0.f)) continue;
+          const int k = atomicAdd(&sm.hq_n[0], 1);
+          if (k < hq_cap) {
+            sm.hq[k] = make_int2(c * ns + si, p);
+            continue;
+          }
+          clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, want_dist ? m + cutoff : m, g, sd, mag);
+        } else {
+          clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, 0.f, g, sd, mag);
+        }
         sdmin = fminf(sdmin, sd);
         if (!check) continue;
         const float mm = margin32(mag);
@@ -313,7 +460,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         }
       }
       if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
-      if (want_dist) dist32[(c0 + c) * ns + si] = sdmin;
+      if (want_dist) sm.sdist[c * ns + si] = f2o(sdmin);
     } else {
       const int u = t - n_sph_tasks;
       const int c = u / npr, pi = u - c * npr;
@@ -349,6 +496,57 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     }
   }
   __syncthreads();
+  // ---- 3b. queued cloud queries, one warp per query
+  {
+    const int lane = tid & 31;
+    const int nq = min(sm.hq_n[0], hq_cap);
+    for (;;) {
+      int k = 0;
+      if (lane == 0) k = atomicAdd(&sm.hq_n[1], 1);
+      k = __shfl_sync(0xffffffffu, k, 0);
+      if (k >= nq) break;
+      const int2 e = sm.hq[k];
+      const int c = e.x / ns, si = e.x - c * ns;
+      const SphereF S = sm.sph[si];
+      const GroupF& G = sm.grp[S.group];
+      const bool check = !G.only_self;
+      // warp-uniform: flags change under other warps, so lane 0 decides for the warp
+      const int done_c = __shfl_sync(0xffffffffu, (!want_dist && (sm.flags[c] & FLAG_FAIL)) ? 1 : 0, 0);
+      if (done_c) continue;
+      const PrimF& Pr = sm.prm[e.y];
+      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * 12;
+      const float3 sc = xf(P, S.x, S.y, S.z);
+      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z));
+      const float reach = Pr.a + S.r + (want_dist ? m + cutoff : m);
+      const NNResult32 nn = warp_nearest32(v.C[Pr.cloud], sc.x, sc.y, sc.z, reach * reach);
+      if (lane == 0) {
+        float g, sd, mag;
+        if (nn.idx < 0) {
+          g = reach - Pr.a - S.r;
+          sd = 3.0e38f;
+          mag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
+        } else {
+          const float d = sqrtf(nn.d2);
+          g = d - Pr.a - S.r;
+          sd = g;
+          mag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z) + d;
+        }
+        if (want_dist) atomicMin(&sm.sdist[c * ns + si], f2o(sd));
+        if (check) {
+          const float mm = margin32(mag);
+          if (g < -mm) {
+            atomicOr(&sm.flags[c], FLAG_FAIL);
+          } else if (g <= mm) {
+            push_item(scr, src, (int)(c0 + c), e.y << 1, si, 0);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (want_dist)
+    for (int t = tid; t < ncfg * ns; t += blockDim.x) dist32[(c0 + t / ns) * ns + t % ns] = o2f(sm.sdist[t]);
+  __syncthreads();
   if (tid < ncfg && !(sm.flags[tid] & 2)) src.done(c0 + tid, (sm.flags[tid] & FLAG_FAIL) != 0);
   __syncthreads();
 }
@@ -371,6 +569,12 @@ __device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
   p += sizeof(unsigned) * cpb * T->n_groups;
   p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
   sm.qbuf = reinterpret_cast<double*>(p);
+  p += sizeof(double) * cpb * T->q_dim;
+  sm.hq_n = reinterpret_cast<int*>(p);
+  p += 16;
+  sm.hq = reinterpret_cast<int2*>(p);  // only with a point cloud
+  if (T->n_clouds > 0) p += sizeof(int2) * cpb * T->n_spheres;
+  sm.sdist = reinterpret_cast<int*>(p);  // only with distance output
   return sm;
 }
 
@@ -426,8 +630,8 @@ __device__ void stage_tables(const TView& v, const Smem& sm) {
   __syncthreads();
 }
 
-template <int CPB>
-__global__ void __launch_bounds__(128) k_fast_valid(const PmTablesHdr* __restrict__ T, const double* __restrict__ state,
+template <int CPB, int NT>
+__global__ void __launch_bounds__(NT) k_fast_valid(const PmTablesHdr* __restrict__ T, const double* __restrict__ state,
                                                     const double* __restrict__ q, int64_t B, uint8_t* __restrict__ out,
                                                     float* __restrict__ dist32, float cutoff, Scratch scr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -440,8 +644,8 @@ __global__ void __launch_bounds__(128) k_fast_valid(const PmTablesHdr* __restric
 }
 
 // Persistent work-queue kernel over the flattened waypoints of all edges.
-template <int CPB>
-__global__ void __launch_bounds__(128) k_fast_edges(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, EdgeSource src,
+template <int CPB, int NT>
+__global__ void __launch_bounds__(NT) k_fast_edges(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, EdgeSource src,
                                                     unsigned long long* next, Scratch scr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long long chunk;
@@ -478,9 +682,27 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
         const PmGroup& g = v.G[v.sgroup[it.z]];
         const DM3 R = qmat(pose[g.slot].q);
         const D3 gc = add(mv(R, D3{g.rel[0], g.rel[1], g.rel[2]}), pose[g.slot].t);
-        if (!outside_aabb(P, gc, g.radius) && !prim_outside(P, v.C, gc, g.radius)) {
-          const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
-          hit = !outside_aabb(P, c, v.sr[it.z]) && !prim_outside(P, v.C, c, v.sr[it.z]);
+        const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
+        const double r = v.sr[it.z];
+        if (P.kind == PM_SDF_CLOUD) {
+          // the sphere's own test first (small reach); its nearest point then settles the gate
+          // exactly unless rounding leaves it undecided: min_p |gc - p| <= |gc - p_near|
+          const PmGridDev& Gd = v.C[P.cloud];
+          bool test = !outside_aabb(P, c, r);
+          int near = -1;
+          if (test) {
+            const double reach = (r + P.a) * (1.0 + 1e-12) + 1e-12;
+            const NNResult64 nn = grid_nearest64(Gd, c, reach * reach);
+            test = nn.idx >= 0 && !(sqrt(nn.d2) - P.a > r);
+            near = nn.idx;
+          }
+          if (test && !outside_aabb(P, gc, g.radius)) {
+            const D3 d{Gd.px[near] - gc.x, Gd.py[near] - gc.y, Gd.pz[near] - gc.z};
+            const double d2n = d.x * d.x + (d.y * d.y + d.z * d.z);
+            hit = !(sqrt(d2n) - P.a > g.radius) || !prim_outside(P, v.C, gc, g.radius);
+          }
+        } else if (!outside_aabb(P, gc, g.radius) && !prim_outside(P, v.C, gc, g.radius)) {
+          hit = !outside_aabb(P, c, r) && !prim_outside(P, v.C, c, r);
         }
       } else {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test
         const int pr = it.y >> 1;
@@ -578,42 +800,77 @@ __global__ void k_scan1(const int32_t* __restrict__ n, int64_t E, int64_t* __res
 
 namespace pmg {
 
-size_t fast_smem_bytes(const PmTablesHdr& h, int cpb) {
+size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist) {
   return sizeof(float) * 12 * (size_t)cpb * h.n_slots + sizeof(SphereF) * h.n_spheres + sizeof(GroupF) * h.n_groups +
          sizeof(PrimF) * h.n_prims + sizeof(int2) * h.n_pairs + sizeof(int) * cpb + sizeof(unsigned) * (size_t)cpb * h.n_groups + 16 +
-         sizeof(double) * (size_t)cpb * h.q_dim;
+         sizeof(double) * (size_t)cpb * h.q_dim + 16 + (h.n_clouds > 0 ? sizeof(int2) * (size_t)cpb * h.n_spheres : 0) +
+         (want_dist ? sizeof(int) * (size_t)cpb * h.n_spheres : 0);
+}
+
+static cudaError_t upload_offsets() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  std::vector<std::pair<float, char4>> v;
+  for (int z = -kOffR; z <= kOffR; z++)
+    for (int y = -kOffR; y <= kOffR; y++)
+      for (int x = -kOffR; x <= kOffR; x++) {
+        const float gx = (float)std::max(std::abs(x) - 1, 0), gy = (float)std::max(std::abs(y) - 1, 0), gz = (float)std::max(std::abs(z) - 1, 0);
+        // exact-below lower bound: rounded down by one part in 1e6
+        const float lb = std::sqrt(gx * gx + gy * gy + gz * gz) * (1.0f - 1e-6f);
+        v.push_back({lb, make_char4((char)x, (char)y, (char)z, 0)});
+      }
+  std::stable_sort(v.begin(), v.end(), [](const std::pair<float, char4>& a, const std::pair<float, char4>& b) {
+    if (a.first != b.first) return a.first < b.first;
+    const int da = a.second.x * a.second.x + a.second.y * a.second.y + a.second.z * a.second.z;
+    const int db = b.second.x * b.second.x + b.second.y * b.second.y + b.second.z * b.second.z;
+    return da < db;
+  });
+  std::vector<char4> off(v.size());
+  std::vector<float> lb(v.size());
+  for (size_t i = 0; i < v.size(); i++) {
+    off[i] = v[i].second;
+    lb[i] = v[i].first;
+  }
+  cudaError_t e = cudaMemcpyToSymbol(c_off, off.data(), off.size() * sizeof(char4));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_off_lb, lb.data(), lb.size() * sizeof(float));
+  if (e == cudaSuccess) done = true;
+  return e;
 }
 
 template <class K>
 static cudaError_t prep(K kern, size_t sm) {
+  cudaError_t e = upload_offsets();
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
 }
 
 // count, overflow and stats must be zeroed by the caller
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
-                              uint8_t* overflow, unsigned long long* stats, int cpb, cudaStream_t s) {
+                              uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s) {
   if (B <= 0) return cudaSuccess;
   Scratch scr{items, count, cap, overflow, stats};
-  size_t sm = fast_smem_bytes(h, cpb);
+  size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
   cudaError_t e;
   prof_begin("k_fast_valid", s);
-  switch (cpb) {
-    case 16:
-      if ((e = prep(k_fast_valid<16>, sm)) != cudaSuccess) return e;
-      k_fast_valid<16><<<grid, 128, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);
-      break;
-    case 64:
-      if ((e = prep(k_fast_valid<64>, sm)) != cudaSuccess) return e;
-      k_fast_valid<64><<<grid, 128, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);
-      break;
-    default:
-      if ((e = prep(k_fast_valid<32>, sm)) != cudaSuccess) return e;
-      k_fast_valid<32><<<grid, 128, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);
-      break;
+#define PM_FAST_CASE(C, N)                                                                      \
+  if (cpb == C && nt == N) {                                                                     \
+    if ((e = prep(k_fast_valid<C, N>, sm)) != cudaSuccess) return e;                             \
+    k_fast_valid<C, N><<<grid, N, sm, s>>>(T, state, q, B, out, dist32, cutoff, scr);            \
+    launched = true;                                                                             \
   }
+  bool launched = false;
+  PM_FAST_CASE(16, 128)
+  PM_FAST_CASE(32, 128)
+  PM_FAST_CASE(32, 256)
+  PM_FAST_CASE(64, 256)
+  PM_FAST_CASE(32, 512)
+  PM_FAST_CASE(64, 512)
+  PM_FAST_CASE(128, 512)
+#undef PM_FAST_CASE
+  if (!launched) return cudaErrorInvalidValue;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_end("k_fast_valid", s);
   CfgSource src{q, B, out};
@@ -637,14 +894,14 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   k_scan1<<<1, 1024, 0, s>>>(n, E, off);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   EdgeSource src{s1, s2, off, n, sr, seq, E, out};
-  size_t sm = fast_smem_bytes(h, cpb);
+  size_t sm = fast_smem_bytes(h, cpb, false);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   int per_sm = 0;
-  if ((e = prep(k_fast_edges<32>, sm)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<32>, 128, sm)) != cudaSuccess) return e;
+  if ((e = prep(k_fast_edges<32, 128>, sm)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<32, 128>, 128, sm)) != cudaSuccess) return e;
   unsigned grid = (unsigned)(n_sm * (per_sm > 0 ? per_sm : 1));
   prof_begin("k_fast_edges", s);
-  k_fast_edges<32><<<grid, 128, sm, s>>>(T, state, src, next, scr);
+  k_fast_edges<32, 128><<<grid, 128, sm, s>>>(T, state, src, next, scr);
   prof_end("k_fast_edges", s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_begin("k_fast_recheck_edges", s);

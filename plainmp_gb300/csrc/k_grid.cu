@@ -165,6 +165,48 @@ __global__ void k_edf_pass(const int32_t* __restrict__ blk_occ, const int16_t* _
     out[c[0] + nbx * (c[1] + nby * c[2])] = (int16_t)best;
   }
 }
+// occupancy of fine cells in x-fastest order (counts are stored block-major)
+__global__ void k_cell_occ(const int32_t* __restrict__ count, int ncx, int ncy, int ncz, int nbx, int nby, uint8_t* __restrict__ occ) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)ncx * ncy * ncz) return;
+  const int cx = (int)(i % ncx), cy = (int)((i / ncx) % ncy), cz = (int)(i / ((int64_t)ncx * ncy));
+  const int b = (cx / PM_GRID_B) + nbx * ((cy / PM_GRID_B) + nby * (cz / PM_GRID_B));
+  const int l = (cx % PM_GRID_B) + PM_GRID_B * ((cy % PM_GRID_B) + PM_GRID_B * (cz % PM_GRID_B));
+  occ[i] = count[(int64_t)b * PM_GRID_CELLS_PER_BLOCK + l] > 0 ? 1 : 0;
+}
+// Separable squared distance transform between cell boxes: per-axis cost max(|i - j| - 1, 0)^2
+// summed over axes (the squared gap between two unit cells), minimised over occupied cells.
+__global__ void k_bdt_pass(const uint8_t* __restrict__ occ, const int32_t* __restrict__ in, int32_t* __restrict__ out, int nx, int ny,
+                           int nz, int axis) {
+  const int n[3] = {nx, ny, nz};
+  const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+  int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= n[a1] * n[a2]) return;
+  int c[3];
+  c[a1] = line % n[a1];
+  c[a2] = line / n[a1];
+  c[axis] = 0;
+  const int len = n[axis];
+  const int64_t stride = axis == 0 ? 1 : (axis == 1 ? (int64_t)nx : (int64_t)nx * ny);
+  const int64_t base = c[0] + (int64_t)nx * (c[1] + (int64_t)ny * c[2]);
+  const int INF = 0x3fffffff;
+  for (int i = 0; i < len; i++) {
+    int best = INF;
+    for (int j = 0; j < len; j++) {
+      const int64_t b = base + j * stride;
+      const int v = axis == 0 ? (occ[b] ? 0 : INF) : in[b];
+      if (v >= INF) continue;
+      const int gap = max(abs(i - j) - 1, 0);
+      best = min(best, v + gap * gap);
+    }
+    out[base + i * stride] = best;
+  }
+}
+__global__ void k_bdt_final(const int32_t* __restrict__ d2, int64_t n, double cell, float* __restrict__ lb) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  lb[i] = d2[i] >= 0x3fffffff ? INFINITY : __double2float_rd(sqrt((double)d2[i]) * cell);
+}
 __global__ void k_edf_final(const int16_t* __restrict__ in, int64_t n, uint8_t* __restrict__ edf) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) edf[i] = (uint8_t)min((int)in[i], 255);
@@ -206,6 +248,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   float4* p32 = nullptr;
   int32_t *blk_occ = nullptr, *cell_pts = nullptr;
   uint8_t* edf = nullptr;
+  float* cell_lb = nullptr;
   float *blk_box = nullptr, *cell_box = nullptr;
   int32_t n_rec = 0;
   do {
@@ -257,6 +300,21 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       k_edf_final<<<nblk(nblocks, 256), 256, 0, s>>>(t0, nblocks, edf);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
+    {  // Euclidean lower-bound field on fine cells
+      const int64_t ncl = (int64_t)nc[0] * nc[1] * nc[2];
+      int32_t *t0 = nullptr, *t1 = nullptr;
+      uint8_t* occ = nullptr;
+      if ((e = scratch(ncl * 4, (void**)&t0)) != cudaSuccess) break;
+      if ((e = scratch(ncl * 4, (void**)&t1)) != cudaSuccess) break;
+      if ((e = scratch(ncl, (void**)&occ)) != cudaSuccess) break;
+      if ((e = keep(ncl * 4, (void**)&cell_lb)) != cudaSuccess) break;
+      k_cell_occ<<<nblk(ncl, 256), 256, 0, s>>>(count, nc[0], nc[1], nc[2], nb[0], nb[1], occ);
+      k_bdt_pass<<<nblk((int64_t)nc[1] * nc[2], 64), 64, 0, s>>>(occ, nullptr, t0, nc[0], nc[1], nc[2], 0);
+      k_bdt_pass<<<nblk((int64_t)nc[0] * nc[2], 64), 64, 0, s>>>(occ, t0, t1, nc[0], nc[1], nc[2], 1);
+      k_bdt_pass<<<nblk((int64_t)nc[0] * nc[1], 64), 64, 0, s>>>(occ, t1, t0, nc[0], nc[1], nc[2], 2);
+      k_bdt_final<<<nblk(ncl, 256), 256, 0, s>>>(t0, ncl, g.cell, cell_lb);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+    }
     e = cudaStreamSynchronize(s);
   } while (false);
   for (void* p : tmp) cudaFree(p);
@@ -273,6 +331,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.cell_box = cell_box;
   d.cell_pts = cell_pts;
   d.edf = edf;
+  d.cell_lb = cell_lb;
   d.n_points = (int32_t)n;
   return cudaSuccess;
 }

@@ -78,10 +78,11 @@ struct PmGridDev {
   const float* cell_box;   // per occupied cell: lo xyz, hi xyz
   const int32_t* cell_pts; // per occupied cell: [first point, end)
   const uint8_t* edf;      // per block: Chebyshev distance in blocks to the nearest occupied block (capped at 255)
+  const float* cell_lb;    // per fine cell (x fastest): lower bound (m) on the distance from the cell to any point
   int32_t nbx, nby, nbz;   // blocks per axis
   int32_t n_points;
   double origin[3];        // grid origin (world)
-  double block;            // block edge length
+  double block;            // block edge length (PM_GRID_B fine cells)
   double lb[3], ub[3];     // CloudSDF AABB (point bounds -/+ radius)
   double radius;
 };
