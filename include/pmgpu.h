@@ -186,6 +186,18 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
 int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block);
 int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* threads_per_block);
 
+/* Fast path for callers that must not allocate device memory during the call (real-time loops,
+ * devices whose memory another allocator owns, code that cannot afford cudaMalloc's implicit
+ * synchronisation).  No counterpart in the reference.  Same results as pmgpu_cst_is_valid_fast
+ * with PMGPU_MEM_DEVICE: q, out and dist32 (optional) are device pointers and the work is
+ * enqueued on `stream`.  Its scratch is a fixed file-scope device array of about 2 MB (held on
+ * every device that loads the library until exit); the first call on a device looks up that
+ * array's address, so make it before any stream capture.  Requirements and limits: B <= 1048576
+ * (larger batches return PMGPU_ERR_INVALID); the constraint's tables must already be on the
+ * device from an earlier batch call (else PMGPU_ERR_RUNTIME, never an allocation); calls that
+ * overlap on the GPU share the scratch array and race.  Error text: pmgpu_last_error(). */
+int pmgpu_cst_is_valid_fast_noalloc(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, void* stream);
+
 /* ---------------------------------------------------------------- motion validator
  * CustomValidatorBase::checkMotion(s1, s2) (ompl/motion_validator.cpp:17-79) for E edges
  * with BoxMotionValidator (type 0, width[q_dim], :89-111) or EuclideanMotionValidator

@@ -810,6 +810,10 @@ struct HostCst {
   }
 };
 
+// Device view of a constraint whose tables and model state already live on the device
+// (built by an earlier batch call); false instead of building them.  Allocates nothing.
+bool cst_device_view(pmgpu_cst* c, const PmTablesHdr** T, PmTablesHdr* hdr, const double** state, int* cpb, int* nt);
+
 }  // namespace pmg
 
 // ============================================================================ C ABI
@@ -1544,6 +1548,28 @@ int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int hig
     cuda_check(cudaStreamSynchronize(s), "sphere distances");
   });
 }
+}  // extern "C"
+namespace pmg {
+void set_last_error(const char* msg) { g_last_error = msg; }
+bool cst_device_view(pmgpu_cst* c, const PmTablesHdr** T, PmTablesHdr* hdr, const double** state, int* cpb, int* nt) {
+  HostCst& C = c->c;
+  if (!C.d_tables.p || !C.kin->dev_ready || C.sig_model_version != C.kin->version) return false;
+  std::vector<std::shared_ptr<HostSdf>> f;
+  if (C.fixed_sdf) flatten(C.fixed_sdf, f);
+  if (C.sdf) flatten(C.sdf, f);
+  std::vector<std::pair<const HostSdf*, uint64_t>> s;
+  for (auto& x : f) s.push_back({x.get(), x->version});
+  if (s != C.sig) return false;  // the scene changed since the tables were built
+  *T = C.d_tables.as<PmTablesHdr>();
+  *hdr = C.hdr;
+  *state = C.kin->d_state.as<double>();
+  *cpb = C.fast_cpb;
+  *nt = C.fast_nt;
+  return true;
+}
+}  // namespace pmg
+extern "C" {
+
 int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block) {
   return guarded([&] {
     check_ptr(c, "cst");
