@@ -62,6 +62,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     extra = ["-Xptxas", "-v"] if ptxas_info else []
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, digest, extra if s.suffix == ".cu" else []), srcs))
+    for stale in set(BUILD.glob("*.o")) - set(objs):  # objects of earlier source versions
+        stale.unlink()
     link_tag = hashlib.sha1("".join(o.name for o in objs).encode()).hexdigest()[:16]
     stamp = BUILD / f"link.{link_tag}"
     if LIB.exists() and stamp.exists():
