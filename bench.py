@@ -146,6 +146,192 @@ def cpu_baseline(robot, scene, q, seconds: float = 6.0):
             "sample": f"{done} configs of the same batch ({reps} x {n}), validity only (the reference has no per-sphere distance output)"}
 
 
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
+
+
+def _timer(dev, flush, stream):
+    import torch
+
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, n):
+        """Mean ms of fn over n runs, L2 flushed before each, CUDA events on torch's stream."""
+        fn()
+        torch.cuda.synchronize(dev)
+        tt = 0.0
+        for _ in range(n):
+            flush.fill_(1.0)
+            torch.cuda.synchronize(dev)
+            start.record(stream)
+            fn()
+            end.record(stream)
+            end.synchronize()
+            tt += start.elapsed_time(end)
+        return tt / n
+
+    return timed
+
+
+def bench_chain7(dev, timed):
+    """C0 (4096 configurations) and C1 (1024 edges of 1-120 waypoints) on the 7-joint chain
+    against 10 boxes, 5 spheres and 5 cylinders: the plain FP64 method vs the fast path."""
+    import torch
+
+    from plainmp_gb300 import BoxMotionValidator, scenes
+    from plainmp_gb300 import workloads as W
+
+    robot, scene = W.chain7_robot(), W.chain7_scene()
+    _, cst, _ = scenes.make_constraint(robot, scene)
+    Q = torch.tensor(W.chain7_configs(4096), device=dev)
+    ms_plain = timed(lambda: cst.is_valid_batch(Q), 5)
+    ms_fast = timed(lambda: cst.is_valid_fast(Q, distances=True), 10)
+    same = bool(torch.equal(cst.is_valid_fast(Q), cst.is_valid_batch(Q)))
+    s1, s2 = W.chain7_edges(1024)
+    S1, S2 = torch.tensor(s1, device=dev), torch.tensor(s2, device=dev)
+    mv = BoxMotionValidator(cst, [0.05] * 7)
+    ms_e_plain = timed(lambda: mv.check_motion_batch(S1, S2), 5)
+    ms_e_fast = timed(lambda: mv.check_motion_fast(S1, S2), 10)
+    same_e = bool(torch.equal(mv.check_motion_fast(S1, S2), mv.check_motion_batch(S1, S2)))
+    return {
+        "C0": {"workload": "7-joint chain, 56 spheres, 10 boxes + 5 spheres + 5 cylinders, 4096 configurations",
+               "unit": "configs/s", "plain_fp64": 4096 / (ms_plain / 1e3), "fast_with_distances": 4096 / (ms_fast / 1e3),
+               "ms": {"plain_fp64": ms_plain, "fast_with_distances": ms_fast}, "validity_identical": same},
+        "C1": {"workload": "1024 straight edges on the C0 chain and scene, box validator width 0.05 rad, 1-120 waypoints",
+               "unit": "edges/s", "plain_fp64": 1024 / (ms_e_plain / 1e3), "fast_persistent": 1024 / (ms_e_fast / 1e3),
+               "ms": {"plain_fp64": ms_e_plain, "fast_persistent": ms_e_fast}, "edge_validity_identical": same_e},
+    }
+
+
+def _capture(fn):
+    """A CUDA graph of fn (warmed up on a side stream first), or the capture error."""
+    import torch
+
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(2):
+            fn()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    return g
+
+
+def bench_ik(dev, timed, steps=50, lr=0.05):
+    """C3: 8192 collision-aware IK problems on the C0 chain and scene, `steps` gradient steps
+    each.  One gradient eval = cost + adjoint gradient of one problem at one step."""
+    import torch
+
+    from plainmp_gb300 import diff, scenes
+    from plainmp_gb300 import workloads as W
+
+    robot, scene = W.chain7_robot(), W.chain7_scene()
+    kin, cst, _ = scenes.make_constraint(robot, scene)
+    link = kin.get_link_ids([robot.end_link])[0]
+    q0, q_star = W.ik_problems(8192)
+    n = q0.shape[0]
+    tgt = diff.link_poses(cst, torch.tensor(q_star, device=dev), link).float()
+    Q0 = torch.tensor(q0, dtype=torch.float32, device=dev)
+    lo, hi = np.array(kin.get_joint_position_limits(kin.get_joint_ids(robot.control_joints))).T
+    lo_t, hi_t = torch.tensor(lo, dtype=torch.float32, device=dev), torch.tensor(hi, dtype=torch.float32, device=dev)
+    ms_fused = timed(lambda: diff.ik_descend(cst, Q0, tgt, link, steps=steps, lr=lr), 5)
+    c_init = diff.ik_cost_grad(cst, Q0, tgt, link, want_grad=False)
+    _, c_final = diff.ik_descend(cst, Q0, tgt, link, steps=steps, lr=lr)
+    qbuf = Q0.clone()
+
+    def autograd_loop():
+        q = qbuf
+        for _ in range(steps):
+            qq = q.detach().requires_grad_(True)
+            c = diff.ik_cost(cst, qq, tgt, link)
+            (g,) = torch.autograd.grad(c.sum(), qq)
+            q = torch.minimum(torch.maximum(q - lr * g, lo_t), hi_t)
+        return q
+
+    ms_eager = timed(autograd_loop, 2)
+    graph = None
+    try:
+        graph = _capture(autograd_loop)
+        ms_graph = timed(graph.replay, 5)
+    except Exception as e:  # noqa: BLE001 - reported in the JSON line
+        ms_graph = None
+        graph_err = f"{type(e).__name__}: {e}"
+    evals = n * steps
+    # algorithmic flops per eval (no broad phase, no early exit): forward FK 7 x 90 + 8 links x 24,
+    # 56 sphere transforms x 18, narrow phase 56 x (35 x 10 boxes + 11 x 5 spheres + 30 x 5
+    # cylinders); forward + adjoint counted as 3 x forward
+    fwd = 7 * 90 + 8 * 24 + 56 * 18 + 56 * (35 * 10 + 11 * 5 + 30 * 5)
+    flops = 3 * fwd
+    achieved = evals * flops / (ms_fused / 1e3) / 1e12
+    out = {
+        "workload": "8192 IK problems, 7-joint chain (56 spheres) vs 10 boxes + 5 spheres + 5 cylinders, "
+                    f"{steps} gradient steps, lr {lr}, cost |p-p*|^2 + 0.1 |log(R*^T R)|^2 + sum max(0, 0.02 - d_s)^2",
+        "unit": "gradient evals/s",
+        "fused_descent": evals / (ms_fused / 1e3),
+        "autograd_eager": evals / (ms_eager / 1e3),
+        "autograd_cuda_graph": evals / (ms_graph / 1e3) if ms_graph else None,
+        "ms": {"fused_descent": ms_fused, "autograd_eager": ms_eager, "autograd_cuda_graph": ms_graph},
+        "median_cost": {"initial": float(c_init.median()), "after_descent": float(c_final.median())},
+        "roofline": {"bound": "fp32 issue", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                     "frac": achieved / FP32_NOMINAL_TFLOPS, "peak_kind": "nominal (FP32 FMA, 2.07 GHz)",
+                     "flops_per_eval": flops, "kernel": "k_ik_cost (fused descent)"},
+    }
+    if ms_graph is None:
+        out["autograd_cuda_graph_error"] = graph_err
+    return out
+
+
+def bench_traj(dev, timed):
+    """C4: 512 trajectories (20-100 waypoints) of the planar-base chain (x, y, yaw + 7 joints)
+    against the 200k-point cloud; one eval = cost + gradient of one trajectory (FK recomputed
+    in the backward pass), through the torch.autograd.Function, captured in a CUDA graph."""
+    import torch
+
+    from plainmp_gb300 import diff, scenes
+    from plainmp_gb300 import workloads as W
+
+    robot = W.planar_chain7_robot()
+    scene = W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0)
+    _, cst, _ = scenes.make_constraint(robot, scene)
+    trajs = W.trajectories(512)
+    Qh = np.concatenate(trajs, axis=0).astype(np.float32)
+    off = np.concatenate([[0], np.cumsum([len(t) for t in trajs])]).astype(np.int64)
+    Q = torch.tensor(Qh, device=dev)
+    O = torch.tensor(off, device=dev)
+    gout = torch.empty_like(Q)
+    cout = torch.empty(len(trajs), device=dev)
+
+    def fwd_bwd():
+        q = Q.detach().requires_grad_(True)
+        c = diff.trajectory_cost(cst, q, O)
+        (g,) = torch.autograd.grad(c.sum(), q)
+        gout.copy_(g)
+        cout.copy_(c)
+
+    ms_eager = timed(fwd_bwd, 5)
+    try:
+        graph = _capture(fwd_bwd)
+        ms_graph = timed(graph.replay, 10)
+        err = None
+    except Exception as e:  # noqa: BLE001
+        ms_graph, err = None, f"{type(e).__name__}: {e}"
+    ms_direct = timed(lambda: diff.traj_cost_grad(cst, Q, O), 10)
+    best = ms_graph or ms_eager
+    out = {
+        "workload": f"512 trajectories, {len(Qh)} waypoints (20-100 each), planar base + 7 joints (56 spheres) vs the "
+                    "200k-point cloud, hinge margin 0.03 + acceleration smoothing",
+        "unit": "trajectory gradient evals/s",
+        "value": len(trajs) / (best / 1e3),
+        "waypoints_per_s": len(Qh) / (best / 1e3),
+        "ms": {"autograd_eager": ms_eager, "autograd_cuda_graph": ms_graph, "cost_and_grad_one_call": ms_direct},
+    }
+    if err:
+        out["autograd_cuda_graph_error"] = err
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -185,6 +371,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true", help="skip the C0/C1/C3/C4 side measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -312,6 +499,13 @@ def main():
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
 
+    side = None
+    if rank == 0 and not args.headline_only:
+        timed2 = _timer(dev, flush, stream)
+        side = bench_chain7(dev, timed2)
+        side["C3"] = bench_ik(dev, timed2)
+        side["C4"] = bench_traj(dev, timed2)
+
     if rank != 0:
         return
     cpu = None if args.no_cpu_baseline else cpu_baseline(robot, scene, qh)
@@ -345,6 +539,8 @@ def main():
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if side is not None:
+        line["workloads"] = side
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

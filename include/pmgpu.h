@@ -211,6 +211,52 @@ int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t
 int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type,
                             const double* width, double resolution, uint8_t* out, int64_t* stats, int mem, void* stream);
 
+/* ---------------------------------------------------------------- link poses
+ * World pose (x y z qx qy qz qw) of `link` for B configurations, FP64, the FK of
+ * ConstraintBase::update_kintree with std::sin/std::cos (constraints/primitive.hpp:38-62)
+ * followed by KinematicModel::get_link_pose (kinematics/kinematics.hpp:131-140). */
+int pmgpu_cst_link_poses(pmgpu_cst* c, int32_t link, const double* q, int64_t B, double* out7, int mem, void* stream);
+
+/* ---------------------------------------------------------------- differentiable costs
+ * FP32 costs with gradients from a hand-written reverse-mode adjoint (FK chain + SDF).  No
+ * counterpart in the reference, whose IK (src/plainmp/ik.py:42-156) and smoother
+ * (src/plainmp/nlp_solver/sqp_based_solver.py) call the FP64 constraint Jacobians from a CPU solver; the
+ * terms reuse its definitions:
+ *   d_s       = min over primitives of SDF.evaluate(centre_s) - r_s (the ext row's value,
+ *               constraints/primitive_sphere_collision.cpp:256-322), spheres of self-only groups
+ *               excluded;
+ *   hinge     = w_col * sum_s max(0, margin - d_s)^2;
+ *   pose      = w_pos * ||p - p*||^2 + w_rot * ||log(R*^T R)||^2 of pose_link;
+ *   smoothing = w_smooth * sum_t sum_d w_d^2 (q[t+1] - 2 q[t] + q[t-1])_d^2, the acceleration
+ *               cost of smoothcost_fullmat (nlp_solver/sqp_based_solver.py:74-97).
+ * PMGPU_COST_MIN_DISTANCE instead returns min(cutoff, min_s d_s) and its gradient, the value and
+ * Jacobian row of SphereCollisionCst's ext row (analytic instead of finite differences). */
+#define PMGPU_COST_SUM 0
+#define PMGPU_COST_MIN_DISTANCE 1
+typedef struct pmgpu_cost_params {
+  int32_t mode;              /* PMGPU_COST_SUM | PMGPU_COST_MIN_DISTANCE */
+  int32_t pose_link;         /* link id of the pose term, -1: none */
+  float w_pos, w_rot;        /* defaults 1, 0.1 */
+  float w_col, margin;       /* defaults 1, 0.02 */
+  float cutoff;              /* MIN_DISTANCE clamp, default 0.1 */
+  float w_smooth;            /* trajectories, default 1 */
+  const float* dof_weights;  /* host, q_dim entries (w_d), NULL = ones */
+} pmgpu_cost_params;
+/* IK batch: q B x q_dim, target B x 7 (x y z qx qy qz qw; NULL when there is no pose term);
+ * cost[B]; grad B x q_dim or NULL (cost only). */
+int pmgpu_ik_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, const float* target, int64_t B, float* cost,
+                  float* grad, int mem, void* stream);
+/* `steps` gradient-descent steps q <- q - lr * grad(q) per problem inside one launch (clamped to
+ * the joint limits when clamp_to_limits); q is updated in place, cost[B] (optional) receives the
+ * final cost and cost_hist B x steps (optional) the cost before each step. */
+int pmgpu_ik_descend(pmgpu_cst* c, const pmgpu_cost_params* p, float* q, const float* target, int64_t B, int32_t steps,
+                     float lr, int32_t clamp_to_limits, float* cost, float* cost_hist, int mem, void* stream);
+/* Trajectory batch: q n_waypoints x q_dim (trajectories back to back), offsets[n_traj + 1]
+ * (int64, offsets[0] = 0, offsets[n_traj] = n_waypoints); cost[n_traj]; grad n_waypoints x q_dim
+ * or NULL.  FK is recomputed per waypoint for the gradient; nothing is stored between calls. */
+int pmgpu_traj_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, const int64_t* offsets, int64_t n_traj,
+                    int64_t n_waypoints, float* cost, float* grad, int mem, void* stream);
+
 /* ---------------------------------------------------------------- instrumentation
  * Opt-in timing of the library's own kernels: when enabled, CUDA events are recorded around
  * every kernel launch on the stream it is launched on.  pmgpu_profile_read synchronises,

@@ -1610,6 +1610,28 @@ int orc_cst_evaluate(void* p, const double* q, long long B, double* vals, double
 }
 // per-sphere signed distance min_k (sdf_k.evaluate(c) - r) over all flattened SDFs (no cutoff,
 // no gates); plus the sphere centres (high_accuracy selects the FK sin/cos)
+// World pose [x y z qx qy qz qw] of `link` after update_kintree(q, high_accuracy=true)
+// (constraints/primitive.hpp:38-62, kinematics/kinematics.hpp:131-136), for B configurations.
+int orc_cst_link_poses(void* p, const double* q, long long B, int link, double* out7, int nthreads) {
+  auto* oc = (OrcCst*)p;
+  size_t d = oc->c.q_dim();
+  ORC_TRY(parallel_for(B, nthreads, [&](int, long long b, long long e) {
+    CstState st = oc->fresh();
+    for (long long i = b; i < e; i++) {
+      update_kintree(*oc->c.m, st.kin, oc->c.ids, oc->c.base_type, q + i * d, true);
+      const QT& t = link_pose(*oc->c.m, st.kin, link);
+      double* o = out7 + i * 7;
+      o[0] = t.t.x;
+      o[1] = t.t.y;
+      o[2] = t.t.z;
+      o[3] = t.q.x;
+      o[4] = t.q.y;
+      o[5] = t.q.z;
+      o[6] = t.q.w;
+    }
+  }))
+}
+
 int orc_cst_sphere_distances(void* p, const double* q, long long B, int high_accuracy, double* dist, double* centres, int nthreads) {
   auto* oc = (OrcCst*)p;
   size_t d = oc->c.q_dim();

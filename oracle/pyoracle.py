@@ -284,6 +284,12 @@ class Cst:
         lib().orc_cst_dims(h, C.byref(qd), C.byref(cd), C.byref(ns))
         self.q_dim, self.n_spheres = qd.value, ns.value
         self.n_groups = len(specs)
+        # per sphere: its group is self-only (group order is the spec order; reordering is within a group)
+        self._self_only = np.repeat(np.array([bool(s.only_self_collision) for s in specs], dtype=bool), counts) \
+            if specs else np.zeros(0, dtype=bool)
+
+    def sphere_self_only(self) -> np.ndarray:
+        return self._self_only
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -330,6 +336,13 @@ class Cst:
         cen = np.empty((Q.shape[0], self.n_spheres, 3))
         _chk(lib().orc_cst_sphere_distances(self.h, _d(Q), C.c_longlong(Q.shape[0]), int(high_accuracy), _d(dist), _d(cen), threads))
         return (dist, cen) if centres else dist
+
+    def link_poses(self, Q, link: int, threads: int = 1) -> np.ndarray:
+        """(B, 7) [x y z qx qy qz qw] of `link` after update_kintree(q, high_accuracy=True)."""
+        Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1, self.q_dim)
+        out = np.empty((Q.shape[0], 7))
+        _chk(lib().orc_cst_link_poses(self.h, _d(Q), C.c_longlong(Q.shape[0]), int(link), _d(out), threads))
+        return out
 
     def check_motion(self, S1, S2, kind: int = 0, width=None, resolution: float = 0.05, threads: int = 1):
         S1 = np.ascontiguousarray(S1, dtype=np.float64).reshape(-1, self.q_dim)
@@ -384,3 +397,61 @@ def make_constraint(robot, scene=None, self_collision: bool = True, reorder: boo
     if sdf is not None:
         c.set_sdf(sdf)
     return m, c, sdf
+
+
+# ------------------------------------------------------------------ FP64 costs (differentiable paths)
+def _qmul(a, b):
+    ax, ay, az, aw = np.moveaxis(a, -1, 0)
+    bx, by, bz, bw = np.moveaxis(b, -1, 0)
+    return np.stack([aw * bx + ax * bw + ay * bz - az * by, aw * by + ay * bw + az * bx - ax * bz,
+                     aw * bz + az * bw + ax * by - ay * bx, aw * bw - ax * bx - ay * by - az * bz], axis=-1)
+
+
+def rotvec_error(q, qt):
+    """phi = log(R(qt)^T R(q)) as a rotation vector (shortest arc), quaternions [x y z w]."""
+    e = _qmul(qt * np.array([-1.0, -1.0, -1.0, 1.0]), q)
+    e = np.where(e[..., 3:4] < 0, -e, e)
+    s = np.linalg.norm(e[..., :3], axis=-1)
+    k = np.where(s > 1e-12, 2.0 * np.arctan2(s, e[..., 3]) / np.maximum(s, 1e-300), 2.0 / e[..., 3])
+    return k[..., None] * e[..., :3]
+
+
+def ik_cost(cst: "Cst", Q, target, link: int, w_pos=1.0, w_rot=0.1, w_col=1.0, margin=0.02, threads: int = 1):
+    """FP64 collision-aware IK cost: w_pos ||p - p*||^2 + w_rot ||log(R*^T R)||^2 of `link`
+    plus w_col sum_s max(0, margin - d_s)^2, d_s the per-sphere min of SDF.evaluate - r
+    (orc_cst_sphere_distances with sin/cos FK).  target: (B, 7) [x y z qx qy qz qw]."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1, cst.q_dim)
+    cost = np.zeros(Q.shape[0])
+    if link >= 0 and target is not None:
+        pose = cst.link_poses(Q, link, threads=threads)
+        T = np.asarray(target, dtype=np.float64).reshape(-1, 7)
+        cost += w_pos * np.sum((pose[:, :3] - T[:, :3]) ** 2, axis=1)
+        cost += w_rot * np.sum(rotvec_error(pose[:, 3:], T[:, 3:]) ** 2, axis=1)
+    if w_col != 0.0:
+        d = cst.sphere_distances(Q, high_accuracy=True, threads=threads)
+        active = ~np.asarray(cst.sphere_self_only(), dtype=bool)
+        h = np.maximum(margin - d[:, active], 0.0)
+        cost += w_col * np.sum(h * h, axis=1)
+    return cost
+
+
+def smooth_cost(Q, dof_weights=None):
+    """sum_t sum_d w_d^2 (q[t+1] - 2 q[t] + q[t-1])_d^2 = x^T A x with A of smoothcost_fullmat
+    (src/plainmp/nlp_solver/sqp_based_solver.py:74-97)."""
+    Q = np.asarray(Q, dtype=np.float64)
+    if Q.shape[0] < 3:
+        return 0.0
+    acc = Q[2:] - 2.0 * Q[1:-1] + Q[:-2]
+    w2 = np.ones(Q.shape[1]) if dof_weights is None else np.asarray(dof_weights, dtype=np.float64) ** 2
+    return float(np.sum(acc * acc * w2))
+
+
+def traj_cost(cst: "Cst", Q, offsets, w_col=1.0, margin=0.03, w_smooth=1.0, dof_weights=None, threads: int = 1):
+    """FP64 per-trajectory cost: w_smooth * smooth_cost + w_col * hinge sum over all waypoints."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1, cst.q_dim)
+    col = ik_cost(cst, Q, None, -1, w_col=w_col, margin=margin, threads=threads)
+    out = np.empty(len(offsets) - 1)
+    for i in range(len(offsets) - 1):
+        a, b = int(offsets[i]), int(offsets[i + 1])
+        out[i] = w_smooth * smooth_cost(Q[a:b], dof_weights) + np.sum(col[a:b])
+    return out

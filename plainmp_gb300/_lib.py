@@ -103,6 +103,10 @@ _SIGS = {
     "pmgpu_check_motion_fast": (_i, [_p, _p, _p, _i64, _i, _p, _d, _p, _p, _i, _p]),
     "pmgpu_cst_set_fast_launch": (_i, [_p, _i, _i]),
     "pmgpu_cst_get_fast_launch": (_i, [_p, C.POINTER(_i), C.POINTER(_i)]),
+    "pmgpu_cst_link_poses": (_i, [_p, C.c_int32, _p, _i64, _p, _i, _p]),
+    "pmgpu_ik_cost": (_i, [_p, _p, _p, _p, _i64, _p, _p, _i, _p]),
+    "pmgpu_ik_descend": (_i, [_p, _p, _p, _p, _i64, C.c_int32, C.c_float, C.c_int32, _p, _p, _i, _p]),
+    "pmgpu_traj_cost": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p, _i, _p]),
     "pmgpu_profile_enable": (_i, [_i]),
     "pmgpu_profile_read": (_i, [C.c_char_p, _dp, _i64p]),
 }
@@ -177,8 +181,9 @@ class Batch:
         except ImportError:  # pragma: no cover
             pass
         if self.torch is not None and x.is_cuda:
-            tdt = {np.float64: self.torch.float64, np.float32: self.torch.float32, np.uint8: self.torch.uint8}[dtype]
-            self.keep = x.to(tdt).contiguous()
+            tdt = {np.float64: self.torch.float64, np.float32: self.torch.float32, np.uint8: self.torch.uint8,
+                   np.int64: self.torch.int64}[dtype]
+            self.keep = x.detach().to(tdt).contiguous()
             self.mem = MEM_DEVICE
             self.ptr = C.c_void_p(self.keep.data_ptr())
             self.stream = C.c_void_p(self.torch.cuda.current_stream(self.keep.device).cuda_stream)
@@ -195,7 +200,8 @@ class Batch:
     def empty(self, shape, dtype):
         """An output buffer in the same memory space."""
         if self.mem == MEM_DEVICE:
-            tdt = {np.float64: self.torch.float64, np.float32: self.torch.float32, np.uint8: self.torch.uint8}[dtype]
+            tdt = {np.float64: self.torch.float64, np.float32: self.torch.float32, np.uint8: self.torch.uint8,
+                   np.int64: self.torch.int64}[dtype]
             t = self.torch.empty(shape, dtype=tdt, device=self.keep.device)
             return t, C.c_void_p(t.data_ptr())
         a = np.empty(shape, dtype=dtype)

@@ -596,7 +596,21 @@ struct HostCst {
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
   DevBuf e_sr, e_n, e_off;            // fast edge path: step ratios, waypoint counts and offsets
+  DevBuf g_wp;                        // trajectory costs: per-waypoint partial costs
   std::vector<int16_t> seq_host;
+  std::vector<int> extra_links;  // links a pose term needs that no sphere chain reaches
+
+  // FK slot of `link`; the link (and its ancestors) joins the tables if it is not there yet.
+  int slot_for_link(int link) {
+    if (link < 0 || link >= kin->n_link()) fail(PMGPU_ERR_INVALID, "link id out of range");
+    tables();
+    if (slot_of_link[link] < 0) {
+      extra_links.push_back(link);
+      d_tables.release();
+      tables();
+    }
+    return slot_of_link[link];
+  }
 
   int q_dim() const { return (int)ids.size() + (base_type == PM_BASE_FLOATING) * 6 + (base_type == PM_BASE_PLANAR) * 3; }
   int n_spheres() const {
@@ -634,6 +648,8 @@ struct HostCst {
     need[m.root] = 1;
     for (auto& g : groups)
       for (int l = g.link; l >= 0; l = m.parent[l]) need[l] = 1;
+    for (int e : extra_links)
+      for (int l = e; l >= 0; l = m.parent[l]) need[l] = 1;
     std::vector<int> links;
     for (int l = 0; l < nl; l++)
       if (need[l]) links.push_back(l);  // DFS numbering puts parents before children
@@ -884,6 +900,36 @@ T* stage_in(DevBuf& buf, const T* host, size_t count, cudaStream_t s) {
 template <class T>
 void stage_out(T* host, const T* dev, size_t count, cudaStream_t s) {
   if (count) cuda_check(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, s), "D2H copy");
+}
+
+GradArgs grad_args(HostCst& C, const pmgpu_cost_params* p, bool want_pose) {
+  GradArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.mode = p ? p->mode : PMGPU_COST_SUM;
+  if (a.mode != PMGPU_COST_SUM && a.mode != PMGPU_COST_MIN_DISTANCE) fail(PMGPU_ERR_INVALID, "unknown cost mode");
+  a.w_pos = p ? p->w_pos : 1.0f;
+  a.w_rot = p ? p->w_rot : 0.1f;
+  a.w_col = p ? p->w_col : 1.0f;
+  a.margin = p ? p->margin : 0.02f;
+  a.cutoff = p ? p->cutoff : 0.1f;
+  a.w_smooth = p ? p->w_smooth : 1.0f;
+  for (float v : {a.w_pos, a.w_rot, a.w_col, a.margin, a.cutoff, a.w_smooth})
+    if (!std::isfinite(v)) fail(PMGPU_ERR_INVALID, "cost parameters must be finite");
+  const int d = C.q_dim();
+  if (d > PM_GRAD_MAXQ) fail(PMGPU_ERR_INVALID, "q_dim above the cost kernels' limit");
+  for (int j = 0; j < PM_GRAD_MAXQ; j++) {
+    const float w = (p && p->dof_weights && j < d) ? p->dof_weights[j] : 1.0f;
+    a.dofw2[j] = w * w;
+    a.lo[j] = -INFINITY;
+    a.hi[j] = INFINITY;
+  }
+  for (size_t c = 0; c < C.ids.size(); c++) {
+    a.lo[c] = (float)C.kin->joints[C.ids[c]].lower;
+    a.hi[c] = (float)C.kin->joints[C.ids[c]].upper;
+  }
+  a.pose_slot = -1;
+  if (want_pose && p && p->pose_link >= 0 && a.mode == PMGPU_COST_SUM) a.pose_slot = C.slot_for_link(p->pose_link);
+  return a;
 }
 
 void check_joint_ids(const HostModel& m, const int64_t* ids, int n) {
@@ -1747,6 +1793,145 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
         stats[2] = (int64_t)h[4];
         stats[3] = 0;
       }
+    }
+  });
+}
+
+// ------------------------------------------------------------------ link poses, differentiable costs
+
+int pmgpu_cst_link_poses(pmgpu_cst* c, int32_t link, const double* q, int64_t B, double* out7, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    HostCst& C = c->c;
+    const int slot = C.slot_for_link(link);
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const double* dq = q;
+    double* dout = out7;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(C.w_in, q, (size_t)B * C.q_dim(), s);
+      dout = (double*)C.w_out.ensure(std::max<size_t>((size_t)B * 7 * 8, 16));
+    }
+    cuda_check(launch_link_pose64(T, st, dq, B, slot, dout, s), "link_poses");
+    if (mem == PMGPU_MEM_HOST) {
+      stage_out(out7, dout, (size_t)B * 7, s);
+      cuda_check(cudaStreamSynchronize(s), "link_poses");
+    }
+  });
+}
+
+int pmgpu_ik_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, const float* target, int64_t B, float* cost,
+                  float* grad, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    check_ptr(cost, "cost");
+    HostCst& C = c->c;
+    GradArgs a = grad_args(C, p, target != nullptr);
+    a.steps = 0;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const int d = C.q_dim();
+    const float* dq = q;
+    const float* dt = target;
+    float* dc = cost;
+    float* dg = grad;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(C.w_in, q, (size_t)B * d, s);
+      if (target) dt = stage_in(C.w_in2, target, (size_t)B * 7, s);
+      dc = (float*)C.w_out.ensure(std::max<size_t>((size_t)B * 4, 16));
+      if (grad) dg = (float*)C.w_out2.ensure(std::max<size_t>((size_t)B * d * 4, 16));
+    }
+    cuda_check(launch_ik_cost(T, C.hdr, st, a, const_cast<float*>(dq), dt, B, dc, dg, nullptr, s), "ik_cost");
+    if (mem == PMGPU_MEM_HOST) {
+      stage_out(cost, dc, (size_t)B, s);
+      if (grad) stage_out(grad, dg, (size_t)B * d, s);
+      cuda_check(cudaStreamSynchronize(s), "ik_cost");
+    }
+  });
+}
+
+int pmgpu_ik_descend(pmgpu_cst* c, const pmgpu_cost_params* p, float* q, const float* target, int64_t B, int32_t steps,
+                     float lr, int32_t clamp_to_limits, float* cost, float* cost_hist, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    if (steps < 1) throw std::invalid_argument("steps must be positive");
+    if (!std::isfinite(lr)) throw std::invalid_argument("lr must be finite");
+    HostCst& C = c->c;
+    GradArgs a = grad_args(C, p, target != nullptr);
+    if (a.mode != PMGPU_COST_SUM) fail(PMGPU_ERR_INVALID, "descent minimises the PMGPU_COST_SUM cost");
+    a.steps = steps;
+    a.lr = lr;
+    a.clamp = clamp_to_limits != 0;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const int d = C.q_dim();
+    float* dq = q;
+    const float* dt = target;
+    float* dc = cost;
+    float* dh = cost_hist;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(C.w_in, (const float*)q, (size_t)B * d, s);
+      if (target) dt = stage_in(C.w_in2, target, (size_t)B * 7, s);
+      if (cost) dc = (float*)C.w_out.ensure(std::max<size_t>((size_t)B * 4, 16));
+      if (cost_hist) dh = (float*)C.w_out2.ensure(std::max<size_t>((size_t)B * steps * 4, 16));
+    }
+    cuda_check(launch_ik_cost(T, C.hdr, st, a, dq, dt, B, dc, nullptr, dh, s), "ik_descend");
+    if (mem == PMGPU_MEM_HOST) {
+      stage_out(q, (const float*)dq, (size_t)B * d, s);
+      if (cost) stage_out(cost, dc, (size_t)B, s);
+      if (cost_hist) stage_out(cost_hist, dh, (size_t)B * steps, s);
+      cuda_check(cudaStreamSynchronize(s), "ik_descend");
+    }
+  });
+}
+
+int pmgpu_traj_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, const int64_t* offsets, int64_t n_traj,
+                    int64_t n_waypoints, float* cost, float* grad, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    check_mem(mem);
+    if (n_traj < 0 || n_waypoints < 0) throw std::invalid_argument("negative count");
+    check_ptr(offsets, "offsets");
+    check_ptr(cost, "cost");
+    if (mem == PMGPU_MEM_HOST) {  // the device clamps offsets into range; host input is checked
+      if (offsets[0] != 0 || offsets[n_traj] != n_waypoints)
+        throw std::invalid_argument("offsets must start at 0 and end at n_waypoints");
+      for (int64_t i = 0; i < n_traj; i++)
+        if (offsets[i + 1] < offsets[i]) throw std::invalid_argument("offsets must be non-decreasing");
+    }
+    HostCst& C = c->c;
+    GradArgs a = grad_args(C, p, false);
+    if (a.mode != PMGPU_COST_SUM) fail(PMGPU_ERR_INVALID, "trajectory costs use PMGPU_COST_SUM");
+    a.steps = 0;
+    const PmTablesHdr* T = C.tables();
+    const double* st = C.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const int d = C.q_dim();
+    float* wp = (float*)C.g_wp.ensure(std::max<size_t>((size_t)n_waypoints * 4, 16));
+    const float* dq = q;
+    const int64_t* doff = offsets;
+    float* dc = cost;
+    float* dg = grad;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(C.w_in, q, (size_t)n_waypoints * d, s);
+      doff = stage_in(C.w_in2, offsets, (size_t)n_traj + 1, s);
+      dc = (float*)C.w_out.ensure(std::max<size_t>((size_t)n_traj * 4, 16));
+      if (grad) dg = (float*)C.w_out2.ensure(std::max<size_t>((size_t)n_waypoints * d * 4, 16));
+    }
+    cuda_check(launch_traj_cost(T, C.hdr, st, a, dq, doff, n_traj, n_waypoints, wp, dc, dg, s), "traj_cost");
+    if (mem == PMGPU_MEM_HOST) {
+      stage_out(cost, dc, (size_t)n_traj, s);
+      if (grad) stage_out(grad, dg, (size_t)n_waypoints * d, s);
+      cuda_check(cudaStreamSynchronize(s), "traj_cost");
     }
   });
 }

@@ -48,6 +48,29 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
                               int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
                               unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int n_sm, cudaStream_t s);
 
+// ---- differentiable costs (k_grad.cu): FP32 forward + reverse-mode adjoint
+#define PM_GRAD_MAXQ (PM_MAX_CTRL + 8)
+struct GradArgs {
+  int mode;       // 0: hinge sum (+ pose term); 1: min signed distance over spheres (the ext row)
+  int pose_slot;  // FK slot of the pose term, -1: none
+  float w_pos, w_rot, w_col, margin, cutoff, w_smooth, lr;
+  int steps;      // > 0: gradient descent of that many steps inside the launch
+  int clamp;      // descent: clamp q to [lo, hi]
+  float lo[PM_GRAD_MAXQ], hi[PM_GRAD_MAXQ], dofw2[PM_GRAD_MAXQ];
+};
+size_t grad_smem_bytes(const PmTablesHdr& h);
+// IK batch: q B x q_dim (updated in place when steps > 0), target B x 7 (x y z qx qy qz qw) or
+// NULL; cost B (final cost after a descent), grad B x q_dim or NULL, hist B x steps or NULL.
+cudaError_t launch_ik_cost(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const GradArgs& a, float* q,
+                           const float* target, int64_t B, float* cost, float* grad, float* hist, cudaStream_t s);
+// Trajectory batch: q n_wp x q_dim, off n_traj + 1 waypoint offsets; wp_cost n_wp scratch.
+cudaError_t launch_traj_cost(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const GradArgs& a, const float* q,
+                             const int64_t* off, int64_t n_traj, int64_t n_wp, float* wp_cost, float* cost, float* grad,
+                             cudaStream_t s);
+// FP64 world pose (x y z qx qy qz qw) of one FK slot for B configurations (sin/cos FK).
+cudaError_t launch_link_pose64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int slot, double* out7,
+                               cudaStream_t s);
+
 // ---- SDF utilities (k_plain.cu): prims/clouds describe one SDF (a union is flattened)
 cudaError_t launch_sdf_points(const PmPrim* prims, int n_prims, const PmGridDev* clouds, int is_union, const double* pts,
                               const double* radii, int64_t n, double* eval_out, uint8_t* outside_out, cudaStream_t s);
