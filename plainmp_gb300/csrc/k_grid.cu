@@ -23,7 +23,7 @@ __global__ void k_keys(const double* __restrict__ pts, int64_t n, double ox, dou
   int c[3];
   for (int a = 0; a < 3; a++) {
     double f = floor((p[a] - o[a]) * inv_cell);
-    c[a] = f < 0 ? 0 : (f > nc[a] - 1 ? nc[a] - 1 : (int)f);
+    c[a] = !(f >= 0) ? 0 : (f > nc[a] - 1 ? nc[a] - 1 : (int)f);  // NaN -> 0
   }
   int b = (c[0] / PM_GRID_B) + nbx * ((c[1] / PM_GRID_B) + nby * (c[2] / PM_GRID_B));
   int l = (c[0] % PM_GRID_B) + PM_GRID_B * ((c[1] % PM_GRID_B) + PM_GRID_B * (c[2] % PM_GRID_B));
@@ -239,6 +239,11 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   };
   PmGridDev& d = g.dev;
   const int64_t n = g.n;
+  // the caller sizes the grid (origin, blocks per axis, block edge); refuse a descriptor whose
+  // cell keys would fall outside the count arrays
+  if (!(d.nbx >= 1 && d.nby >= 1 && d.nbz >= 1 && n >= 0 && g.cell > 0.0 && d.block > 0.0) ||
+      (int64_t)d.nbx * d.nby * d.nbz * PM_GRID_CELLS_PER_BLOCK > ((int64_t)1 << 30))
+    return cudaErrorInvalidValue;
   const int nb[3] = {d.nbx, d.nby, d.nbz};
   const int nc[3] = {nb[0] * PM_GRID_B, nb[1] * PM_GRID_B, nb[2] * PM_GRID_B};
   const int64_t nblocks = (int64_t)nb[0] * nb[1] * nb[2];
