@@ -495,11 +495,14 @@ static void build_cloud(CloudData& cd) {
     }
   double cell = cd.cell > 0 ? cd.cell : 0.012;
   double blk = cell * PM_GRID_B;
+  // the grid extends the points' box by the nearest-point field's reach, so queries near the
+  // cloud but outside its box still get the field's bounds
+  const double pad = n > 0 ? cd.g.field_reach : 0.0;
   int nb[3];
   for (;;) {
     int64_t tot = 1;
     for (int a = 0; a < 3; a++) {
-      double ext = n > 0 ? (hi[a] - lo[a]) : 0.0;
+      double ext = n > 0 ? (hi[a] - lo[a]) + 2.0 * pad : 0.0;
       nb[a] = (int)std::floor(ext / blk) + 1;
       tot *= nb[a];
     }
@@ -515,7 +518,7 @@ static void build_cloud(CloudData& cd) {
   g.dev.nbx = nb[0];
   g.dev.nby = nb[1];
   g.dev.nbz = nb[2];
-  for (int a = 0; a < 3; a++) g.dev.origin[a] = n > 0 ? lo[a] : 0.0;
+  for (int a = 0; a < 3; a++) g.dev.origin[a] = n > 0 ? lo[a] - pad : 0.0;
   g.dev.block = blk;
   g.dev.radius = cd.radius;
   for (int a = 0; a < 3; a++) {

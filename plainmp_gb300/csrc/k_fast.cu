@@ -1,8 +1,9 @@
 // FP32 fast path with FP64 recheck (validity booleans identical to the plain method).
 //
 // Per block of CPB configurations:
-//   1. FK in FP64 (the plain path's exact arithmetic), each slot's rotation matrix and
-//      translation rounded once to FP32 into shared memory;
+//   1. FK in FP32 into shared memory, with a running bound on each slot's error against the
+//      FP64 FK of the reference (see fk32); every later margin adds the bound of the spheres
+//      involved;
 //   2. group culling: the clearance of each sphere group's bounding sphere against each
 //      primitive (a point cloud: a radius-bounded FP32 nearest-neighbour query);
 //   3. sphere tasks (sphere x primitive) and self-pair tasks (group pair x sphere pairs), each
@@ -19,6 +20,7 @@
 #include <cmath>
 #include <vector>
 
+#include "pm_grad.cuh"
 #include "pm_launch.h"
 #include "pm_view.cuh"
 
@@ -40,12 +42,30 @@ struct PrimF {
 struct SphereF {
   float x, y, z, r;
   int group, tiny;  // tiny: the FP64 radius is below 1e-6 (the reference's special cases)
+  float sn;         // |offset in the link frame|, rounded up (for the FK error bound)
 };
 struct GroupF {
   float rel[3], radius;
   int slot, begin, count, only_self;
-  int tiny, pad[3];
+  int tiny;
+  float gn;  // |group centre in the link frame|, rounded up
+  int pad[2];
 };
+
+// FP32 FK slot: the local transform's constant part (joint origin, or the fixed transform of a
+// slot without a control joint, taken from the model state when the block starts).
+struct SlotF {
+  int parent, mode, qcol, lid;
+  float axis[3];
+  float lq[4];
+  float lt[3];
+  float lt1;  // |lt|_1 (prismatic: of the origin part)
+};
+// Per slot and configuration in shared memory: [0..8] R, [9..11] t, [12] et = bound on |t - t64|,
+// [13] eb = bound on |R - R64| as an operator (8 eq + 24 u), [14..17] world quaternion,
+// [18] eq = bound on |q - q64|_2.  A point s of the link frame then lies within et + eb |s| of
+// its FP64 position, plus the rounding of R s + t that margin32 covers.
+constexpr int kPoseF = 20;
 
 enum { ST_PASS = 0, ST_FAIL = 1, ST_MAYBE = 2 };
 constexpr int FLAG_FAIL = 1;
@@ -61,6 +81,121 @@ struct Scratch {
 __device__ __forceinline__ float3 xf(const float* P, float x, float y, float z) {  // R (row-major 9) * v + t (P[9..11])
   return make_float3(fmaf(P[0], x, fmaf(P[1], y, fmaf(P[2], z, P[9]))), fmaf(P[3], x, fmaf(P[4], y, fmaf(P[5], z, P[10]))),
                      fmaf(P[6], x, fmaf(P[7], y, fmaf(P[8], z, P[11]))));
+}
+
+// compute_approx_sin_cos (kinematics/algorithm.cpp:50-86) with the range reduction in FP64 and
+// the polynomial in FP32 (Horner form): within 8 units of roundoff (sin) and 12 (cos) of the FP64
+// value for the reduced |x| <= pi/2.
+__device__ __forceinline__ void approx_sin_cos32(double x, float& s, float& c) {
+  const double pi = 3.14159265358979323846, half_pi = pi * 0.5;
+  double cos_sign = 1.0;
+  if (x > half_pi || x < -half_pi) {
+    if (x > pi || x < -pi) x = x - 2 * pi * floor(x * (1.0 / (2 * pi)) + 0.5);
+    if (x < -half_pi) {
+      x = -x - pi;
+      cos_sign = -1.0;
+    } else if (x > half_pi) {
+      x = -x + pi;
+      cos_sign = -1.0;
+    }
+  }
+  const float xf = (float)x, xx = xf * xf;
+  s = xf * (1.0f - xx * (1.0f / 6.0f - xx * (1.0f / 120.0f - xx * (1.0f / 5040.0f - xx * (1.0f / 362880.0f)))));
+  c = 1.0f - xx * (0.5f - xx * (1.0f / 24.0f - xx * (1.0f / 720.0f - xx * (1.0f / 40320.0f))));
+  if (cos_sign < 0.0) c = -c;
+}
+
+// FP32 FK of one configuration into P (n_slots x kPoseF) with error bounds against the FP64 FK
+// of the reference (update_kintree + get_link_pose; algorithm.cpp:88-210).  Bounds, u = 2^-24,
+// norms 2-norms, quaternions within 1e-3 of unit norm:
+//   local rotation: joint quaternion from sin/cos (Taylor: 8u / 12u; sincosf: 2 ulp + the
+//     rounding of x) and an FP32 axis: 20u; times the FP32 origin quaternion: 32u;
+//   composition q = qp (x) lq: |dq| <= 1.001 (|dqp| + |dlq|) + 8.1u (4-term fused sums);
+//   rotation of a vector v by an FP32 matrix of qp: |d(Rv)| <= (8 |dqp| + 24u) |v| (the map
+//     q -> R(q)v has derivative norm <= 6.4 |v| at |q| <= 1.001; matrix and product rounding);
+//   translation t = tp + R lt: |dt| <= |dtp| + (8 |dqp| + 24u)|lt| + 1.01 u (|tp|_1 + |lt|_1).
+// The base pose adds the rounding of q's base entries (and of their half angles).
+__device__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restrict__ base8, int base_type, int n_ctrl,
+                     const double* __restrict__ q, bool taylor, float* __restrict__ P) {
+  for (int i = 0; i < nsl; i++) {
+    const SlotF s = S[i];
+    float* o = P + i * kPoseF;
+    FQ wq;
+    float wt[3], eq, et;
+    if (s.parent < 0) {
+      if (base_type == PM_BASE_PLANAR) {
+        const double hy = q[n_ctrl + 2] * 0.5;
+        float sy, cy;
+        sincosf((float)hy, &sy, &cy);
+        wq = FQ{0.f, 0.f, sy, cy};
+        wt[0] = (float)q[n_ctrl];
+        wt[1] = (float)q[n_ctrl + 1];
+        wt[2] = 0.f;
+        eq = kU * (8.0f + 2.0f * fabsf((float)hy));
+      } else if (base_type == PM_BASE_FLOATING) {
+        const double hr = q[n_ctrl + 3] * 0.5, hp = q[n_ctrl + 4] * 0.5, hy = q[n_ctrl + 5] * 0.5;
+        float sr, cr, sp, cp, sy, cy;
+        sincosf((float)hr, &sr, &cr);
+        sincosf((float)hp, &sp, &cp);
+        sincosf((float)hy, &sy, &cy);
+        wq = FQ{sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy, cr * cp * cy + sr * sp * sy};
+        for (int k = 0; k < 3; k++) wt[k] = (float)q[n_ctrl + k];
+        eq = kU * (40.0f + 4.0f * (fabsf((float)hr) + fabsf((float)hp) + fabsf((float)hy)));
+      } else {
+        wq = FQ{base8[0], base8[1], base8[2], base8[3]};
+        for (int k = 0; k < 3; k++) wt[k] = base8[4 + k];
+        eq = 2.0f * kU;
+      }
+      et = kU * (fabsf(wt[0]) + fabsf(wt[1]) + fabsf(wt[2]));
+    } else {
+      const float* pp = P + s.parent * kPoseF;
+      const FQ pq{pp[14], pp[15], pp[16], pp[17]};
+      FQ lq{0.f, 0.f, 0.f, 1.f};
+      float lt[3] = {s.lt[0], s.lt[1], s.lt[2]};
+      float el = 0.f, elt = kU * s.lt1, lt1 = s.lt1;
+      bool lid = s.lid != 0;
+      if (s.mode == PM_FK_STATE) {
+        lq = FQ{s.lq[0], s.lq[1], s.lq[2], s.lq[3]};
+        el = 2.0f * kU;
+      } else if (s.mode == PM_FK_PRIS) {
+        const float th = (float)q[s.qcol];
+        for (int k = 0; k < 3; k++) lt[k] = fmaf(s.axis[k], th, s.lt[k]);
+        lt1 = fabsf(lt[0]) + fabsf(lt[1]) + fabsf(lt[2]);
+        elt = 4.0f * kU * (s.lt1 + fabsf(th) * (fabsf(s.axis[0]) + fabsf(s.axis[1]) + fabsf(s.axis[2])));
+        lid = true;
+      } else {
+        const double x = q[s.qcol] * 0.5;
+        float sn, cs;
+        if (taylor) {
+          approx_sin_cos32(x, sn, cs);
+        } else {
+          sincosf((float)x, &sn, &cs);
+        }
+        const FQ jq{sn * s.axis[0], sn * s.axis[1], sn * s.axis[2], cs};
+        lq = lid ? jq : fqmul(FQ{s.lq[0], s.lq[1], s.lq[2], s.lq[3]}, jq);
+        el = (lid ? 20.0f : 32.0f) * kU + (taylor ? 0.0f : 2.0f * kU * fabsf((float)x));
+        lid = false;
+      }
+      wq = lid ? pq : fqmul(pq, lq);
+      for (int k = 0; k < 3; k++)
+        wt[k] = pp[9 + k] + fmaf(pp[3 * k], lt[0], fmaf(pp[3 * k + 1], lt[1], pp[3 * k + 2] * lt[2]));
+      const float peq = pp[18];
+      eq = lid ? peq + el : 1.001f * (peq + el) + 8.1f * kU;
+      const float nlt = sqrtf(fmaf(lt[0], lt[0], fmaf(lt[1], lt[1], lt[2] * lt[2]))) * 1.001f;
+      et = pp[12] + nlt * pp[13] + 1.01f * kU * (fabsf(pp[9]) + fabsf(pp[10]) + fabsf(pp[11]) + lt1) + elt;
+    }
+    fqmat(wq, o);
+    o[9] = wt[0];
+    o[10] = wt[1];
+    o[11] = wt[2];
+    o[12] = et;
+    o[13] = 8.0f * eq + 24.0f * kU;
+    o[14] = wq.x;
+    o[15] = wq.y;
+    o[16] = wq.z;
+    o[17] = wq.w;
+    o[18] = eq;
+  }
 }
 
 // Clearance g (the reference reports a collision iff g <= 0, up to its own rounding), the
@@ -150,19 +285,23 @@ constexpr int kOffN = (2 * kOffR + 1) * (2 * kOffR + 1) * (2 * kOffR + 1);
 __device__ char4 c_off[kOffN];     // global memory: lanes read different entries
 __device__ float c_off_lb[kOffN];
 
-// Warp-cooperative bounded nearest neighbour (FP32): all 32 lanes call it with the same query.
+// Warp-cooperative bounded nearest neighbour (FP32): all 32 lanes call it with the same query
+// (and the same optional starting candidate).
 // Blocks are visited nearest-first, 32 offsets at a time, until the next offset's lower bound
 // clears the current best; every block that may hold a point below the best is handed to all
 // lanes, which split its occupied cells and test their points; the warp minimum is shared after
 // every block.  Result: the exact minimum of the FP32 squared distances below maxd2 (among
 // equal values the smallest sorted index), as grid_nearest32.
-__device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2) {
+__device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2, float init_d2 = INFINITY,
+                                            int init_idx = -1) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   NNResult32 r{maxd2, -1};
   if (G.n_points <= 0) return r;
-  float best = maxd2;
-  int bidx = -1;
+  // a known point (init_idx at init_d2, e.g. the nearest point of the query's field cell) starts the
+  // walk with a tight bound
+  float best = init_d2 < maxd2 ? init_d2 : maxd2;
+  int bidx = init_d2 < maxd2 ? init_idx : -1;
   const float reach = sqrtf(maxd2);
   const float blk = (float)G.block;
   const float inv = (float)(1.0 / G.block);
@@ -254,6 +393,86 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
   return r;
 }
 
+// Warp-cooperative exact FP64 nearest neighbour below maxd2 (the value of grid_nearest64: the
+// minimum over points of fl(dx*dx + (dy*dy + dz*dz)), pruned by the same conservative boxes).
+// The cube of blocks around q within sqrt(maxd2), one block of slack per side for the rounding
+// of the block assignment, is split across lanes; a candidate block's occupied cells are split
+// across lanes and the warp minimum is shared after every block.  For the few FP64 rechecks,
+// where a single thread's walk would be a long serial chain of FP64 operations and loads.
+__device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, double maxd2) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  NNResult64 r{maxd2, -1};
+  if (G.n_points <= 0 || !(maxd2 > 0.0)) return r;
+  double best = maxd2;
+  int bidx = -1;
+  const double reach = sqrt(maxd2);
+  const double qa[3] = {q.x, q.y, q.z};
+  const int nb[3] = {G.nbx, G.nby, G.nbz};
+  int lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    const double f0 = floor((qa[a] - reach - G.origin[a]) / G.block) - 1.0;
+    const double f1 = floor((qa[a] + reach - G.origin[a]) / G.block) + 1.0;
+    if (!(f1 >= 0.0) || !(f0 <= (double)(nb[a] - 1))) return r;  // also rejects NaN
+    lo[a] = f0 < 0.0 ? 0 : (int)f0;
+    hi[a] = f1 > (double)(nb[a] - 1) ? nb[a] - 1 : (int)f1;
+  }
+  const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+  const int nblk = nx * ny * nz;
+  for (int base = 0; base < nblk; base += 32) {
+    const int i = base + lane;
+    bool cand = false;
+    int2 occ = make_int2(0, 0);
+    if (i < nblk) {
+      const int bx = lo[0] + i % nx;
+      const int t = i / nx;
+      const int by = lo[1] + t % ny, bz = lo[2] + t / ny;
+      const int b = bx + nb[0] * (by + nb[1] * bz);
+      occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + b);
+      cand = occ.x < occ.y && box_d2_64(G.blk_box + 6 * b, q) < best;
+    }
+    unsigned bal = __ballot_sync(FULL, cand);
+    while (bal) {
+      const int src = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const int c0 = __shfl_sync(FULL, occ.x, src), c1 = __shfl_sync(FULL, occ.y, src);
+      for (int c = c0 + lane; c < c1; c += 32) {
+        if (box_d2_64(G.cell_box + 6 * c, q) >= best) continue;
+        const int2 pr = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + c);
+        for (int p = pr.x; p < pr.y; p++) {
+          const D3 d{G.px[p] - q.x, G.py[p] - q.y, G.pz[p] - q.z};
+          const double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
+          if (d2 < best) {
+            best = d2;
+            bidx = p;
+          }
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(FULL, best, o);
+        const int oi = __shfl_xor_sync(FULL, bidx, o);
+        if (ob < best || (ob == best && oi >= 0 && (bidx < 0 || oi < bidx))) {
+          best = ob;
+          bidx = oi;
+        }
+      }
+    }
+  }
+  r.d2 = best;
+  r.idx = bidx;
+  return r;
+}
+
+// is_outside(p, r) of a point cloud (primitive_sdf.hpp:597-603) with the warp search: only
+// whether a point lies within r + radius matters (see prim_outside).  Warp-uniform arguments.
+__device__ __forceinline__ bool cloud_outside_warp(const PmPrim& P, const PmGridDev* clouds, const D3& p, double r, int* near) {
+  const double reach = (r + P.a) * (1.0 + 1e-12) + 1e-12;
+  const NNResult64 nn = warp_nearest64(clouds[P.cloud], p, reach * reach);
+  if (near) *near = nn.idx;
+  if (nn.idx < 0) return true;
+  return sqrt(nn.d2) - P.a > r;
+}
+
 __device__ __forceinline__ int f2o(float f) {
   const int i = __float_as_int(f);
   return i >= 0 ? i : i ^ 0x7fffffff;
@@ -275,7 +494,9 @@ struct Smem {
   int2* hq;      // hard cloud queries: (cfg * n_spheres + sphere, primitive)
   int* hq_n;     // [0] pushed, [1] popped
   int* sdist;    // per (cfg, sphere): running minimum signed distance, order-preserving int
-  float* pose;   // [cfg][slot][12]
+  float* pose;   // [cfg][slot][kPoseF]
+  SlotF* slot;
+  float* base8;  // fixed base pose: q xyzw, t xyz
   SphereF* sph;
   GroupF* grp;
   PrimF* prm;
@@ -365,22 +586,13 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   const int ns = T->n_spheres, ng = T->n_groups, np = T->n_prims, npr = T->n_pairs, nsl = T->n_slots;
   const int tid = threadIdx.x;
   if (tid < CPB) sm.flags[tid] = 0;
-  // ---- 1. FK (FP64, exact) -> FP32 poses
+  // ---- 1. FK (FP32, with error bounds) -> shared memory
   if (tid < ncfg) {
     if (src.pre_skip(c0 + tid)) {
       sm.flags[tid] = FLAG_FAIL | 2;  // already known invalid: no work
     } else {
-      DPose pose[PM_MAX_SLOTS];
       const double* qc = src.cfg(T, c0 + tid, qbuf + tid * T->q_dim);
-      fk64(T, state, qc, T->base_type == PM_BASE_FIXED, pose);
-      float* o = sm.pose + (size_t)tid * nsl * 12;
-      for (int i = 0; i < nsl; i++) {
-        DM3 R = qmat(pose[i].q);
-        for (int k = 0; k < 9; k++) o[12 * i + k] = (float)R.m[k];
-        o[12 * i + 9] = (float)pose[i].t.x;
-        o[12 * i + 10] = (float)pose[i].t.y;
-        o[12 * i + 11] = (float)pose[i].t.z;
-      }
+      fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, sm.pose + (size_t)tid * nsl * kPoseF);
     }
   }
   __syncthreads();
@@ -390,21 +602,22 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     const int c = t / ng, gi = t - c * ng;
     if (sm.flags[c] & 2) continue;
     const GroupF& G = sm.grp[gi];
-    const float* P = sm.pose + ((size_t)c * nsl + G.slot) * 12;
+    const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
     float3 gc = xf(P, G.rel[0], G.rel[1], G.rel[2]);
+    const float ekg = P[12] + P[13] * G.gn;  // FK error bound of the group centre
     unsigned mask = 0;
     const int npc = np < 32 ? np : 32;
     for (int p = 0; p < npc; p++) {
       float g, sd, mag;
       const PrimF& P = sm.prm[p];
-      if (P.kind == PM_SDF_CLOUD) {  // the block distance field bounds the cloud from below
-        const float lb = grid_lower_bound32(v.C[P.cloud], gc.x, gc.y, gc.z);
+      if (P.kind == PM_SDF_CLOUD) {  // the nearest-point field bounds the cloud from below
+        const float lb = grid_field32(v.C[P.cloud], gc.x, gc.y, gc.z).lb;
         g = lb - P.a - G.radius;
         mag = fabsf(gc.x) + fabsf(gc.y) + fabsf(gc.z) + lb;
       } else {
         clearance(P, v.C, gc.x, gc.y, gc.z, G.radius, G.tiny, 0.f, g, sd, mag);
       }
-      if (g > margin32(mag) + (want_dist ? cutoff : 0.f)) mask |= 1u << p;
+      if (g > margin32(mag) + ekg + (want_dist ? cutoff : 0.f)) mask |= 1u << p;
     }
     sm.cull[c * ng + gi] = mask;
   }
@@ -427,19 +640,31 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       const GroupF& G = sm.grp[S.group];
       const bool check = !G.only_self && np > 0;
       if (!want_dist && (!check || (sm.flags[c] & FLAG_FAIL))) continue;
-      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * 12;
+      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
       const float3 sc = xf(P, S.x, S.y, S.z);
+      const float ek = P[12] + P[13] * S.sn;  // FK error bound of the sphere centre
       const unsigned cm = sm.cull[c * ng + S.group];
       float sdmin = cutoff;
       int fail = 0;
-      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z));
+      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
       for (int p = 0; p < np; p++) {
         if (p < 32 && ((cm >> p) & 1u)) continue;
         const PrimF& Pr = sm.prm[p];
         float g, sd, mag;
         if (Pr.kind == PM_SDF_CLOUD) {
-          const float lb = grid_cell_lower_bound32(v.C[Pr.cloud], sc.x, sc.y, sc.z);
-          if (lb - Pr.a - S.r > margin32(fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z) + lb) + (want_dist ? cutoff : 0.f)) continue;
+          const PmGridDev& Gc = v.C[Pr.cloud];
+          const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z);
+          const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
+          if (fb.lb - Pr.a - S.r > margin32(qmag + fb.lb) + ek + (want_dist ? cutoff : 0.f)) continue;
+          if (!want_dist && check && fb.idx >= 0) {
+            // the centre's nearest point is a real point: if it is certainly within reach, the
+            // sphere collides and no search is needed
+            const float ub = sqrtf(point_d2_32(Gc, fb.idx, sc.x, sc.y, sc.z));
+            if (ub - Pr.a - S.r < -(margin32(qmag + ub) + ek)) {
+              fail = 1;
+              break;
+            }
+          }
           const int k = atomicAdd(&sm.hq_n[0], 1);
           if (k < hq_cap) {
             sm.hq[k] = make_int2(c * ns + si, p);
@@ -451,7 +676,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         }
         sdmin = fminf(sdmin, sd);
         if (!check) continue;
-        const float mm = margin32(mag);
+        const float mm = margin32(mag) + ek;
         if (g < -mm) {
           fail = 1;
           if (!want_dist) break;
@@ -468,13 +693,15 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       const int2 pr = sm.pairs[pi];
       const GroupF& G1 = sm.grp[pr.x];
       const GroupF& G2 = sm.grp[pr.y];
-      const float* P1 = sm.pose + ((size_t)c * nsl + G1.slot) * 12;
-      const float* P2 = sm.pose + ((size_t)c * nsl + G2.slot) * 12;
+      const float* P1 = sm.pose + ((size_t)c * nsl + G1.slot) * kPoseF;
+      const float* P2 = sm.pose + ((size_t)c * nsl + G2.slot) * kPoseF;
       const float3 a = xf(P1, G1.rel[0], G1.rel[1], G1.rel[2]);
       const float3 bb = xf(P2, G2.rel[0], G2.rel[1], G2.rel[2]);
       const float ddx = a.x - bb.x, ddy = a.y - bb.y, ddz = a.z - bb.z;
       const float gmag = fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(bb.x) + fabsf(bb.y) + fabsf(bb.z);
-      if (sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz))) - (G1.radius + G2.radius) > 2.0f * margin32(gmag)) continue;
+      if (sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz))) - (G1.radius + G2.radius) >
+          2.0f * margin32(gmag) + P1[12] + P1[13] * G1.gn + P2[12] + P2[13] * G2.gn)
+        continue;
       int fail = 0;
       for (int i = G1.begin; i < G1.begin + G1.count && !fail; i++) {
         const SphereF Si = sm.sph[i];
@@ -484,7 +711,8 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
           const float3 cj = xf(P2, Sj.x, Sj.y, Sj.z);
           const float ex = ci.x - cj.x, ey = ci.y - cj.y, ez = ci.z - cj.z;
           const float g = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))) - (Si.r + Sj.r);
-          const float mm = 2.0f * margin32(fabsf(ci.x) + fabsf(ci.y) + fabsf(ci.z) + fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z));
+          const float mm = 2.0f * margin32(fabsf(ci.x) + fabsf(ci.y) + fabsf(ci.z) + fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z)) +
+                           P1[12] + P1[13] * Si.sn + P2[12] + P2[13] * Sj.sn;
           if (g < -mm) {
             fail = 1;
             break;
@@ -514,11 +742,15 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       const int done_c = __shfl_sync(0xffffffffu, (!want_dist && (sm.flags[c] & FLAG_FAIL)) ? 1 : 0, 0);
       if (done_c) continue;
       const PrimF& Pr = sm.prm[e.y];
-      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * 12;
+      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
       const float3 sc = xf(P, S.x, S.y, S.z);
-      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z));
+      const float ek = P[12] + P[13] * S.sn;
+      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
       const float reach = Pr.a + S.r + (want_dist ? m + cutoff : m);
-      const NNResult32 nn = warp_nearest32(v.C[Pr.cloud], sc.x, sc.y, sc.z, reach * reach);
+      const PmGridDev& Gc = v.C[Pr.cloud];
+      const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z);
+      const float d2_0 = fb.idx >= 0 ? point_d2_32(Gc, fb.idx, sc.x, sc.y, sc.z) : INFINITY;
+      const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, d2_0, fb.idx);
       if (lane == 0) {
         float g, sd, mag;
         if (nn.idx < 0) {
@@ -533,7 +765,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         }
         if (want_dist) atomicMin(&sm.sdist[c * ns + si], f2o(sd));
         if (check) {
-          const float mm = margin32(mag);
+          const float mm = margin32(mag) + ek;
           if (g < -mm) {
             atomicOr(&sm.flags[c], FLAG_FAIL);
           } else if (g <= mm) {
@@ -551,36 +783,92 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   __syncthreads();
 }
 
+// Shared-memory layout of a fast block; every array starts on a 16-byte boundary.
+struct SmemLayout {
+  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, hq_n, hq, sdist, total;
+};
+__host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
+__host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb, bool want_dist) {
+  SmemLayout L;
+  size_t o = 0;
+  L.pose = o;
+  o = a16(o + sizeof(float) * kPoseF * (size_t)cpb * h.n_slots);
+  L.slot = o;
+  o = a16(o + sizeof(SlotF) * h.n_slots);
+  L.base8 = o;
+  o = a16(o + sizeof(float) * 8);
+  L.sph = o;
+  o = a16(o + sizeof(SphereF) * h.n_spheres);
+  L.grp = o;
+  o = a16(o + sizeof(GroupF) * h.n_groups);
+  L.prm = o;
+  o = a16(o + sizeof(PrimF) * h.n_prims);
+  L.pairs = o;
+  o = a16(o + sizeof(int2) * h.n_pairs);
+  L.flags = o;
+  o = a16(o + sizeof(int) * cpb);
+  L.cull = o;
+  o = a16(o + sizeof(unsigned) * (size_t)cpb * h.n_groups);
+  L.qbuf = o;
+  o = a16(o + sizeof(double) * (size_t)cpb * h.q_dim);
+  L.hq_n = o;
+  o = a16(o + 16);
+  L.hq = o;
+  o = a16(o + (h.n_clouds > 0 ? sizeof(int2) * (size_t)cpb * h.n_spheres : 0));
+  L.sdist = o;
+  o = a16(o + (want_dist ? sizeof(int) * (size_t)cpb * h.n_spheres : 0));
+  L.total = o;
+  return L;
+}
+
 __device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
+  const SmemLayout L = smem_layout(*T, cpb, true);
   Smem sm;
-  sm.pose = reinterpret_cast<float*>(p);
-  p += sizeof(float) * 12 * cpb * T->n_slots;
-  sm.sph = reinterpret_cast<SphereF*>(p);
-  p += sizeof(SphereF) * T->n_spheres;
-  sm.grp = reinterpret_cast<GroupF*>(p);
-  p += sizeof(GroupF) * T->n_groups;
-  sm.prm = reinterpret_cast<PrimF*>(p);
-  p += sizeof(PrimF) * T->n_prims;
-  sm.pairs = reinterpret_cast<int2*>(p);
-  p += sizeof(int2) * T->n_pairs;
-  sm.flags = reinterpret_cast<int*>(p);
-  p += sizeof(int) * cpb;
-  sm.cull = reinterpret_cast<unsigned*>(p);
-  p += sizeof(unsigned) * cpb * T->n_groups;
-  p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
-  sm.qbuf = reinterpret_cast<double*>(p);
-  p += sizeof(double) * cpb * T->q_dim;
-  sm.hq_n = reinterpret_cast<int*>(p);
-  p += 16;
-  sm.hq = reinterpret_cast<int2*>(p);  // only with a point cloud
-  if (T->n_clouds > 0) p += sizeof(int2) * cpb * T->n_spheres;
-  sm.sdist = reinterpret_cast<int*>(p);  // only with distance output
+  sm.pose = reinterpret_cast<float*>(p + L.pose);
+  sm.slot = reinterpret_cast<SlotF*>(p + L.slot);
+  sm.base8 = reinterpret_cast<float*>(p + L.base8);
+  sm.sph = reinterpret_cast<SphereF*>(p + L.sph);
+  sm.grp = reinterpret_cast<GroupF*>(p + L.grp);
+  sm.prm = reinterpret_cast<PrimF*>(p + L.prm);
+  sm.pairs = reinterpret_cast<int2*>(p + L.pairs);
+  sm.flags = reinterpret_cast<int*>(p + L.flags);
+  sm.cull = reinterpret_cast<unsigned*>(p + L.cull);
+  sm.qbuf = reinterpret_cast<double*>(p + L.qbuf);
+  sm.hq_n = reinterpret_cast<int*>(p + L.hq_n);
+  sm.hq = reinterpret_cast<int2*>(p + L.hq);        // only with a point cloud
+  sm.sdist = reinterpret_cast<int*>(p + L.sdist);   // only with distance output (the last array)
   return sm;
 }
 
-__device__ void stage_tables(const TView& v, const Smem& sm) {
+__device__ void stage_tables(const TView& v, const Smem& sm, const double* __restrict__ state) {
   const PmTablesHdr* T = v.T;
   const int tid = threadIdx.x;
+  for (int i = tid; i < T->n_slots; i += blockDim.x) {
+    const PmSlot& S = v.S[i];
+    SlotF f;
+    f.parent = S.parent;
+    f.mode = S.mode;
+    f.qcol = S.qcol;
+    for (int k = 0; k < 3; k++) f.axis[k] = (float)S.axis[k];
+    double lt[3];
+    if (S.mode == PM_FK_STATE) {
+      const double* r = state + (int64_t)PM_STATE_LINK_ROW(S.link) * PM_STATE_STRIDE;
+      for (int k = 0; k < 4; k++) f.lq[k] = (float)r[k];
+      for (int k = 0; k < 3; k++) lt[k] = r[4 + k];
+      f.lid = r[7] != 0.0;
+    } else {
+      for (int k = 0; k < 4; k++) f.lq[k] = (float)S.oq[k];
+      for (int k = 0; k < 3; k++) lt[k] = S.ot[k];
+      f.lid = S.origin_identity;
+    }
+    for (int k = 0; k < 3; k++) f.lt[k] = (float)lt[k];
+    f.lt1 = (float)((fabs(lt[0]) + fabs(lt[1]) + fabs(lt[2])) * (1.0 + 1e-6));
+    sm.slot[i] = f;
+  }
+  if (tid < 8) {
+    const double* b = state + (int64_t)PM_STATE_BASE_ROW * PM_STATE_STRIDE;
+    sm.base8[tid] = tid < 7 ? (float)b[tid] : 0.0f;
+  }
   for (int i = tid; i < T->n_spheres; i += blockDim.x) {
     SphereF s;
     s.x = (float)v.sx[i];
@@ -589,6 +877,7 @@ __device__ void stage_tables(const TView& v, const Smem& sm) {
     s.r = (float)v.sr[i];
     s.group = v.sgroup[i];
     s.tiny = v.sr[i] < 1e-6;
+    s.sn = (float)(sqrt(v.sx[i] * v.sx[i] + v.sy[i] * v.sy[i] + v.sz[i] * v.sz[i]) * (1.0 + 1e-6));
     sm.sph[i] = s;
   }
   for (int i = tid; i < T->n_groups; i += blockDim.x) {
@@ -603,6 +892,7 @@ __device__ void stage_tables(const TView& v, const Smem& sm) {
     g.count = G.count;
     g.only_self = G.only_self;
     g.tiny = G.radius < 1e-6;
+    g.gn = (float)(sqrt(G.rel[0] * G.rel[0] + G.rel[1] * G.rel[1] + G.rel[2] * G.rel[2]) * (1.0 + 1e-6));
     sm.grp[i] = g;
   }
   for (int i = tid; i < T->n_prims; i += blockDim.x) {
@@ -637,7 +927,7 @@ __global__ void __launch_bounds__(NT) k_fast_valid(const PmTablesHdr* __restrict
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TView v(T);
   Smem sm = carve(smem_raw, T, CPB);
-  stage_tables(v, sm);
+  stage_tables(v, sm, state);
   CfgSource src{q, B, out};
   const int64_t c0 = (int64_t)blockIdx.x * CPB;
   fast_block<CPB>(v, sm, state, src, c0, (int)(B - c0 < CPB ? B - c0 : CPB), dist32, cutoff, scr, sm.qbuf);
@@ -651,7 +941,7 @@ __global__ void __launch_bounds__(NT) k_fast_edges(const PmTablesHdr* __restrict
   __shared__ long long chunk;
   TView v(T);
   Smem sm = carve(smem_raw, T, CPB);
-  stage_tables(v, sm);
+  stage_tables(v, sm, state);
   const int64_t W = src.E > 0 ? src.off[src.E - 1] + src.n[src.E - 1] : 0;
   for (;;) {
     if (threadIdx.x == 0) chunk = (long long)atomicAdd(next, (unsigned long long)CPB);
@@ -667,66 +957,81 @@ __global__ void __launch_bounds__(NT) k_fast_edges(const PmTablesHdr* __restrict
 template <class Src>
 __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, Src src, Scratch scr) {
   TView v(T);
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   const unsigned int n_items = min(*scr.count, scr.cap);
-  const int64_t total = (int64_t)n_items + src.n_overflow_slots();
   double qbuf[PM_MAX_SLOTS + 8];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i < n_items) {
-      const int4 it = scr.items[i];
-      if (src.skip(it.x)) continue;
-      DPose pose[PM_MAX_SLOTS];
-      fk64(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, pose);
-      bool hit = false;
-      if ((it.y & 1) == 0) {  // sphere it.z vs primitive it.y >> 1: gate AND test
-        const PmPrim& P = v.P[it.y >> 1];
-        const PmGroup& g = v.G[v.sgroup[it.z]];
+  // queued terms, one warp per term: lane 0 runs the FP64 FK and the primitive tests, the warp
+  // runs the cloud searches
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < (int64_t)n_items; i += n_warps) {
+    const int4 it = scr.items[i];
+    if (__shfl_sync(FULL, src.skip(it.x) ? 1 : 0, 0)) continue;
+    bool hit = false;
+    if ((it.y & 1) == 0) {  // sphere it.z vs primitive it.y >> 1: gate AND test
+      const PmPrim& P = v.P[it.y >> 1];
+      const PmGroup& g = v.G[v.sgroup[it.z]];
+      double cv[3] = {0, 0, 0}, gv[3] = {0, 0, 0};
+      if (lane == 0) {
+        DPose pose[PM_MAX_SLOTS];
+        fk64(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, pose);
         const DM3 R = qmat(pose[g.slot].q);
         const D3 gc = add(mv(R, D3{g.rel[0], g.rel[1], g.rel[2]}), pose[g.slot].t);
         const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
-        const double r = v.sr[it.z];
-        if (P.kind == PM_SDF_CLOUD) {
-          // the sphere's own test first (small reach); its nearest point then settles the gate
-          // exactly unless rounding leaves it undecided: min_p |gc - p| <= |gc - p_near|
-          const PmGridDev& Gd = v.C[P.cloud];
-          bool test = !outside_aabb(P, c, r);
-          int near = -1;
-          if (test) {
-            const double reach = (r + P.a) * (1.0 + 1e-12) + 1e-12;
-            const NNResult64 nn = grid_nearest64(Gd, c, reach * reach);
-            test = nn.idx >= 0 && !(sqrt(nn.d2) - P.a > r);
-            near = nn.idx;
-          }
-          if (test && !outside_aabb(P, gc, g.radius)) {
-            const D3 d{Gd.px[near] - gc.x, Gd.py[near] - gc.y, Gd.pz[near] - gc.z};
-            const double d2n = d.x * d.x + (d.y * d.y + d.z * d.z);
-            hit = !(sqrt(d2n) - P.a > g.radius) || !prim_outside(P, v.C, gc, g.radius);
-          }
-        } else if (!outside_aabb(P, gc, g.radius) && !prim_outside(P, v.C, gc, g.radius)) {
-          hit = !outside_aabb(P, c, r) && !prim_outside(P, v.C, c, r);
-        }
-      } else {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test
-        const int pr = it.y >> 1;
-        const PmGroup& g1 = v.G[v.pairs[2 * pr]];
-        const PmGroup& g2 = v.G[v.pairs[2 * pr + 1]];
-        const DM3 R1 = qmat(pose[g1.slot].q), R2 = qmat(pose[g2.slot].q);
-        const D3 c1 = add(mv(R1, D3{g1.rel[0], g1.rel[1], g1.rel[2]}), pose[g1.slot].t);
-        const D3 c2 = add(mv(R2, D3{g2.rel[0], g2.rel[1], g2.rel[2]}), pose[g2.slot].t);
-        const double osq = sqn(sub(c1, c2));
-        const double ors = g1.radius + g2.radius;
-        if (!(osq > ors * ors)) {
-          const D3 a = add(mv(R1, v.rel(it.z)), pose[g1.slot].t);
-          const D3 bb = add(mv(R2, v.rel(it.w)), pose[g2.slot].t);
-          const double rs = v.sr[it.z] + v.sr[it.w];
-          hit = sqn(sub(a, bb)) < rs * rs;
-        }
+        cv[0] = c.x;
+        cv[1] = c.y;
+        cv[2] = c.z;
+        gv[0] = gc.x;
+        gv[1] = gc.y;
+        gv[2] = gc.z;
       }
-      if (hit) src.fail(it.x);
-    } else {
-      const int64_t k = i - n_items;
-      if (!scr.overflow[k]) continue;
-      src.full_check(v, state, k, qbuf);
-      atomicAdd(scr.stats + 2, 1ull);
+      for (int k = 0; k < 3; k++) {
+        cv[k] = __shfl_sync(FULL, cv[k], 0);
+        gv[k] = __shfl_sync(FULL, gv[k], 0);
+      }
+      const D3 c{cv[0], cv[1], cv[2]}, gc{gv[0], gv[1], gv[2]};
+      const double r = v.sr[it.z];
+      if (P.kind == PM_SDF_CLOUD) {
+        // the sphere's own test first (small reach); its nearest point then settles the gate
+        // exactly unless rounding leaves it undecided: min_p |gc - p| <= |gc - p_near|
+        const PmGridDev& Gd = v.C[P.cloud];
+        int near = -1;
+        bool test = !outside_aabb(P, c, r) && !cloud_outside_warp(P, v.C, c, r, &near);
+        if (test && !outside_aabb(P, gc, g.radius)) {
+          const D3 d{Gd.px[near] - gc.x, Gd.py[near] - gc.y, Gd.pz[near] - gc.z};
+          const double d2n = d.x * d.x + (d.y * d.y + d.z * d.z);
+          hit = !(sqrt(d2n) - P.a > g.radius) || !cloud_outside_warp(P, v.C, gc, g.radius, nullptr);
+        }
+      } else if (lane == 0 && !outside_aabb(P, gc, g.radius) && !prim_outside(P, v.C, gc, g.radius)) {
+        hit = !outside_aabb(P, c, r) && !prim_outside(P, v.C, c, r);
+      }
+    } else if (lane == 0) {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test
+      DPose pose[PM_MAX_SLOTS];
+      fk64(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, pose);
+      const int pr = it.y >> 1;
+      const PmGroup& g1 = v.G[v.pairs[2 * pr]];
+      const PmGroup& g2 = v.G[v.pairs[2 * pr + 1]];
+      const DM3 R1 = qmat(pose[g1.slot].q), R2 = qmat(pose[g2.slot].q);
+      const D3 c1 = add(mv(R1, D3{g1.rel[0], g1.rel[1], g1.rel[2]}), pose[g1.slot].t);
+      const D3 c2 = add(mv(R2, D3{g2.rel[0], g2.rel[1], g2.rel[2]}), pose[g2.slot].t);
+      const double osq = sqn(sub(c1, c2));
+      const double ors = g1.radius + g2.radius;
+      if (!(osq > ors * ors)) {
+        const D3 a = add(mv(R1, v.rel(it.z)), pose[g1.slot].t);
+        const D3 bb = add(mv(R2, v.rel(it.w)), pose[g2.slot].t);
+        const double rs = v.sr[it.z] + v.sr[it.w];
+        hit = sqn(sub(a, bb)) < rs * rs;
+      }
     }
+    if (__shfl_sync(FULL, hit ? 1 : 0, 0) && lane == 0) src.fail(it.x);
+  }
+  // configurations (or edges) whose terms overflowed the queue: the plain FP64 check, one thread each
+  const int64_t slots = src.n_overflow_slots();
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < slots; k += (int64_t)gridDim.x * blockDim.x) {
+    if (!scr.overflow[k]) continue;
+    src.full_check(v, state, k, qbuf);
+    atomicAdd(scr.stats + 2, 1ull);
   }
 }
 
@@ -800,12 +1105,7 @@ __global__ void k_scan1(const int32_t* __restrict__ n, int64_t E, int64_t* __res
 
 namespace pmg {
 
-size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist) {
-  return sizeof(float) * 12 * (size_t)cpb * h.n_slots + sizeof(SphereF) * h.n_spheres + sizeof(GroupF) * h.n_groups +
-         sizeof(PrimF) * h.n_prims + sizeof(int2) * h.n_pairs + sizeof(int) * cpb + sizeof(unsigned) * (size_t)cpb * h.n_groups + 16 +
-         sizeof(double) * (size_t)cpb * h.q_dim + 16 + (h.n_clouds > 0 ? sizeof(int2) * (size_t)cpb * h.n_spheres : 0) +
-         (want_dist ? sizeof(int) * (size_t)cpb * h.n_spheres : 0);
-}
+size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist) { return smem_layout(h, cpb, want_dist).total; }
 
 static cudaError_t upload_offsets() {
   static bool done = false;

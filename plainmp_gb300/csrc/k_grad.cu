@@ -395,7 +395,12 @@ __device__ __forceinline__ float sphere_min_dist(const Tab& t, const float c[3],
       const PmGridDev& G = t.clouds[P.cloud];
       const float reach = fminf(thr, best) + r + P.a;
       if (!(reach > 0.f)) continue;
-      const NNResult32 nn = grid_nearest32(G, c[0], c[1], c[2], reach * reach);
+      const FieldLB fb = grid_field32(G, c[0], c[1], c[2]);
+      if (fb.lb >= reach) continue;
+      // the field cell's nearest point bounds the walk; the walk reports only strictly closer points
+      const float d2_0 = fb.idx >= 0 ? point_d2_32(G, fb.idx, c[0], c[1], c[2]) : INFINITY;
+      NNResult32 nn = grid_nearest32(G, c[0], c[1], c[2], fminf(reach * reach, d2_0));
+      if (nn.idx < 0 && d2_0 < reach * reach) nn = NNResult32{d2_0, fb.idx};
       if (nn.idx < 0) continue;
       const float4 p = __ldg(G.p32 + nn.idx);
       const float ex = c[0] - p.x, ey = c[1] - p.y, ez = c[2] - p.z;

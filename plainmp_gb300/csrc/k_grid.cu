@@ -8,6 +8,8 @@
 #include "pm_grid.cuh"
 #include "pm_launch.h"
 
+using namespace pmd;
+
 namespace {
 
 constexpr int SCAN_BS = 1024;
@@ -212,6 +214,30 @@ __global__ void k_edf_final(const int16_t* __restrict__ in, int64_t n, uint8_t* 
   if (i < n) edf[i] = (uint8_t)min((int)in[i], 255);
 }
 
+// Nearest-point field: per fine cell, the exact FP32 nearest point of the cell centre within
+// `reach` and a lower bound on the centre's distance to every point (the FP32 value shrunk by the
+// rounding of d^2, of the square root and of the FP32 point coordinates).  Cells whose
+// box-to-box bound already reaches `reach` skip the search.
+__global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int2* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)ncx * ncy * ncz) return;
+  const int cx = (int)(i % ncx), cy = (int)((i / ncx) % ncy), cz = (int)(i / ((int64_t)ncx * ncy));
+  const float cellf = (float)(G.block / PM_GRID_B);
+  const float x = field_centre(G.origin[0], cx, cellf), y = field_centre(G.origin[1], cy, cellf),
+              z = field_centre(G.origin[2], cz, cellf);
+  const float slack = 4e-6f + 2e-7f * (fabsf(x) + fabsf(y) + fabsf(z));
+  float d = reach;
+  int idx = -1;
+  if (G.cell_lb[i] < reach) {
+    const NNResult32 r = grid_nearest32(G, x, y, z, reach * reach);
+    if (r.idx >= 0) {
+      d = sqrtf(r.d2);
+      idx = r.idx;
+    }
+  }
+  out[i] = make_int2(__float_as_int(fmaxf(d * (1.0f - 1e-6f) - slack, 0.0f)), idx);
+}
+
 inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -241,7 +267,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   const int64_t n = g.n;
   // the caller sizes the grid (origin, blocks per axis, block edge); refuse a descriptor whose
   // cell keys would fall outside the count arrays
-  if (!(d.nbx >= 1 && d.nby >= 1 && d.nbz >= 1 && n >= 0 && g.cell > 0.0 && d.block > 0.0) ||
+  if (!(d.nbx >= 1 && d.nby >= 1 && d.nbz >= 1 && n >= 0 && g.cell > 0.0 && d.block > 0.0 && g.field_reach > 0.0) ||
       (int64_t)d.nbx * d.nby * d.nbz * PM_GRID_CELLS_PER_BLOCK > ((int64_t)1 << 30))
     return cudaErrorInvalidValue;
   const int nb[3] = {d.nbx, d.nby, d.nbz};
@@ -254,6 +280,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   int32_t *blk_occ = nullptr, *cell_pts = nullptr;
   uint8_t* edf = nullptr;
   float* cell_lb = nullptr;
+  int2* cell_nn = nullptr;
   float *blk_box = nullptr, *cell_box = nullptr;
   int32_t n_rec = 0;
   do {
@@ -320,6 +347,24 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       k_bdt_final<<<nblk(ncl, 256), 256, 0, s>>>(t0, ncl, g.cell, cell_lb);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
+    {  // nearest-point field (needs the finished descriptor for its nearest-neighbour walks)
+      const int64_t ncl = (int64_t)nc[0] * nc[1] * nc[2];
+      if ((e = keep(ncl * 8, (void**)&cell_nn)) != cudaSuccess) break;
+      PmGridDev v = d;
+      v.px = px;
+      v.py = py;
+      v.pz = pz;
+      v.p32 = p32;
+      v.blk_occ = blk_occ;
+      v.blk_box = blk_box;
+      v.cell_box = cell_box;
+      v.cell_pts = cell_pts;
+      v.edf = edf;
+      v.cell_lb = cell_lb;
+      v.n_points = (int32_t)n;
+      k_field<<<nblk(ncl, 128), 128, 0, s>>>(v, nc[0], nc[1], nc[2], (float)g.field_reach, cell_nn);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+    }
     e = cudaStreamSynchronize(s);
   } while (false);
   for (void* p : tmp) cudaFree(p);
@@ -337,6 +382,8 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.cell_pts = cell_pts;
   d.edf = edf;
   d.cell_lb = cell_lb;
+  d.cell_nn = cell_nn;
+  d.field_reach = (float)g.field_reach;
   d.n_points = (int32_t)n;
   return cudaSuccess;
 }

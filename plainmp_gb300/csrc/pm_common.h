@@ -8,6 +8,7 @@
 // the reference's shared KinematicModel (constraints/primitive.hpp:96).
 #pragma once
 #include <stdint.h>
+#include <vector_types.h>
 
 #define PM_MAX_SLOTS 64   // links one constraint can touch (FK slots)
 #define PM_MAX_CTRL 64    // control joints (relevance bitmask width)
@@ -79,6 +80,11 @@ struct PmGridDev {
   const int32_t* cell_pts; // per occupied cell: [first point, end)
   const uint8_t* edf;      // per block: Chebyshev distance in blocks to the nearest occupied block (capped at 255)
   const float* cell_lb;    // per fine cell (x fastest): lower bound (m) on the distance from the cell to any point
+  const int2* cell_nn;     // per fine cell (x fastest): x = lower bound (m, float bits) on the distance from the
+                           // cell centre to any point, y = sorted index of the centre's nearest point (-1: none
+                           // within field_reach)
+  float field_reach;       // cell_nn searched up to this distance from each centre
+  int32_t pad_nn;
   int32_t nbx, nby, nbz;   // blocks per axis
   int32_t n_points;
   double origin[3];        // grid origin (world)

@@ -193,6 +193,59 @@ __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float 
   return r;
 }
 
+// Centre of fine cell c along one axis.  The build and the queries evaluate this same FP32
+// expression, so a query measures its offset from exactly the point whose distance was stored.
+__device__ __forceinline__ float field_centre(double origin, int c, float cellf) { return (float)origin + ((float)c + 0.5f) * cellf; }
+
+// Nearest-point field of a query q: lb = a lower bound on the distance from q to any point, by the
+// triangle inequality from the distance of a fine-cell centre c (lb = d(c) - |q - c|, any cell
+// would do; the containing one is the tightest); idx = the nearest point of that centre, an upper
+// bound candidate (-1 if none within field_reach, and outside the grid).  Outside the grid, lb is
+// the distance to the box of the points.
+struct FieldLB {
+  float lb;
+  int idx;
+};
+__device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, float qy, float qz) {
+  FieldLB f{INFINITY, -1};
+  if (G.n_points <= 0) return f;
+  const float cellf = (float)(G.block / PM_GRID_B);
+  const float inv = (float)(PM_GRID_B / G.block);
+  const float qa[3] = {qx, qy, qz};
+  const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
+  int cc[3];
+  bool inside = true;
+  for (int a = 0; a < 3; a++) {
+    const float t = floorf((qa[a] - (float)G.origin[a]) * inv);
+    if (!(t >= 0.f && t <= (float)(nc[a] - 1))) inside = false;
+    cc[a] = inside ? (int)t : 0;
+  }
+  if (!inside) {
+    float d2 = 0.f;
+    for (int a = 0; a < 3; a++) {
+      const float lo = __double2float_rd(G.lb[a] + G.radius), hi = __double2float_ru(G.ub[a] - G.radius);
+      const float gap = fmaxf(fmaxf(lo - qa[a], qa[a] - hi), 0.f);
+      d2 = fmaf(gap, gap, d2);
+    }
+    f.lb = fmaxf(sqrtf(d2) * (1.0f - 1e-6f) - 4e-6f, 0.f);
+    return f;
+  }
+  const int2 nn = __ldg(G.cell_nn + cc[0] + nc[0] * (cc[1] + nc[1] * cc[2]));
+  const float dx = qx - field_centre(G.origin[0], cc[0], cellf), dy = qy - field_centre(G.origin[1], cc[1], cellf),
+              dz = qz - field_centre(G.origin[2], cc[2], cellf);
+  const float off = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * (1.0f + 1e-6f) + 1e-7f;
+  f.lb = fmaxf(__int_as_float(nn.x) - off, 0.f);
+  f.idx = nn.y;
+  return f;
+}
+
+// FP32 squared distance from q to point idx, the expression of every nearest-neighbour walk.
+__device__ __forceinline__ float point_d2_32(const PmGridDev& G, int idx, float qx, float qy, float qz) {
+  const float4 p = __ldg(G.p32 + idx);
+  const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
 // Lower bound (FP32, conservative by 4 um) on the distance from q to any cloud point, from the
 // block distance field alone: 0 when q is outside the grid or near an occupied block.
 __device__ __forceinline__ float grid_lower_bound32(const PmGridDev& G, float qx, float qy, float qz) {

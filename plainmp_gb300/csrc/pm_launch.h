@@ -84,6 +84,7 @@ struct GridBuild {
   int64_t n;
   double radius;
   double cell;  // fine cell edge
+  double field_reach = 0.3;  // nearest-point field: search radius around each cell centre
   // outputs (owned by the caller after the call; freed with grid_free)
   PmGridDev dev;
   void* allocs[16];

@@ -103,6 +103,47 @@ def test_fast_near_boundary_rechecks(oracle):
     assert st["rechecked_terms"] >= 10
 
 
+@pytest.mark.parametrize("cloud_radius", [0.0, 0.01])
+def test_fast_cloud_near_boundary(oracle, cloud_radius):
+    """Per configuration, a cloud of three points at r + radius + delta from three robot sphere
+    centres (delta from -3e-3 down to exact tangency and up to +3e-3) plus points on the faces of a
+    3 m cube around the robot: the nearest-point field's shortcuts, the warp search and the FP64
+    recheck must reproduce the reference's decision, and the FP32 distances stay in bound."""
+    robot = W.chain7_robot()
+    n = 36
+    Q = W.chain7_configs(n, seed=41)
+    _, oc0, _ = oracle.make_constraint(robot, None, self_collision=False)
+    _, cen = oc0.sphere_distances(Q, centres=True)
+    radii = oc0.groups()["radii"]
+    rng = np.random.default_rng(5)
+    deltas = [-3e-3, -1e-5, -1e-7, -1e-9, 0.0, 1e-9, 1e-7, 1e-5, 3e-3]
+    faces = rng.uniform(-1.5, 1.5, (1500, 3))
+    ax = rng.integers(0, 3, 1500)
+    faces[np.arange(1500), ax] = np.where(rng.random(1500) < 0.5, -1.5, 1.5)
+    got, ref, rechecked = [], [], 0
+    for b in range(n):
+        pts = []
+        for k, s in enumerate(rng.choice(56, size=3, replace=False)):
+            u = rng.standard_normal(3)
+            u /= np.linalg.norm(u)
+            pts.append(cen[b, s] + u * (radii[s] + cloud_radius + deltas[(b + k) % len(deltas)]))
+        scene = W.Scene(cloud=np.vstack([np.asarray(pts), faces]), cloud_radius=cloud_radius)
+        (_, cst, _), (_, oc, _) = scenes.make_constraint(robot, scene, self_collision=False), \
+            oracle.make_constraint(robot, scene, self_collision=False)
+        q = Q[b:b + 1]
+        r = oc.is_valid(q)
+        ok, st = cst.is_valid_fast(q, stats=True)
+        ok2, d32 = cst.is_valid_fast(q, distances=True)
+        assert np.array_equal(ok, r) and np.array_equal(ok2, r), f"configuration {b}"
+        dref = np.minimum(oc.sphere_distances(q), CUTOFF)
+        assert np.abs(d32.astype(np.float64) - dref).max() < DIST_TOL
+        got.append(int(ok[0]))
+        ref.append(int(r[0]))
+        rechecked += st["rechecked_terms"]
+    assert 0 < sum(ref) < n  # both outcomes occur
+    assert rechecked > 0
+
+
 def test_fast_mobile_base(oracle):
     r = W.chain7_robot()
     r = W.Robot(r.urdf, r.control_joints, r.end_link, r.spheres, r.self_pairs, base_type="PLANAR")
