@@ -343,6 +343,83 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
       bidx = (int)(unsigned)(k & 0xffffffffu);
     }
   };
+  if (inside && G.blk_list) {  // the block's candidate list covers every point within its reach
+    const int b = cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]);
+    const int2 rng = __ldg(G.blk_list + b);
+    if (rng.x >= 0 && sqrtf(best) <= __ldg(G.blk_reach + b)) {
+      // 32 list entries at a time: the occupied cells of every entry whose box is below the best
+      // are concatenated (warp scan of their counts) and split evenly across the lanes
+      for (int base = rng.x; base < rng.y; base += 32) {
+        const int k = base + lane;
+        int2 occ = make_int2(0, 0);
+        int n = 0;
+        bool beyond = true;  // this entry, and (sorted) every later one, lies beyond the best
+        if (k < rng.y) {
+          const int2 e = __ldg(G.blk_cand + k);
+          const float ed = __int_as_float(e.y);
+          beyond = ed * ed * (1.0f - 1e-5f) >= best;
+          if (!beyond) {
+            occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + e.x);
+            if (box_d2_32(G.blk_box + 6 * e.x, qx, qy, qz) < best) n = occ.y - occ.x;
+          }
+        }
+        const bool stop = __shfl_sync(FULL, beyond ? 1 : 0, 31) != 0;
+        int incl = n;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        // up to 4 cells per lane per round: their box loads are independent, so they overlap;
+        // then the point ranges of the surviving cells, then their points
+        for (int t0 = 0; t0 < total; t0 += 128) {
+          int cs[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const int t = t0 + 32 * j + lane;
+            int lo = 0, hi = 31;  // owner: the first lane whose inclusive count exceeds t
+            for (int it = 0; it < 5; it++) {
+              const int mid = (lo + hi) >> 1;
+              if (__shfl_sync(FULL, incl, mid) <= t) lo = mid + 1;
+              else hi = mid;
+            }
+            const int own_first = __shfl_sync(FULL, occ.x, lo), own_excl = __shfl_sync(FULL, incl - n, lo);
+            cs[j] = t < total ? own_first + (t - own_excl) : -1;
+          }
+          int2 pr[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            pr[j] = make_int2(0, 0);
+            if (cs[j] >= 0 && box_d2_32(G.cell_box + 6 * cs[j], qx, qy, qz) < best)
+              pr[j] = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + cs[j]);
+          }
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            for (int p = pr[j].x; p < pr[j].y; p++) {
+              const float4 pt = __ldg(G.p32 + p);
+              const float dx = pt.x - qx, dy = pt.y - qy, dz = pt.z - qz;
+              const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (d2 < best || (d2 == best && bidx >= 0 && p < bidx)) {
+                best = d2;
+                bidx = p;
+              }
+            }
+          }
+        }
+        unsigned long long key = nn_key(best, bidx);
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long k2 = __shfl_xor_sync(FULL, key, o);
+          key = k2 < key ? k2 : key;
+        }
+        best = __uint_as_float((unsigned)(key >> 32));
+        bidx = (int)(unsigned)(key & 0xffffffffu);
+        if (stop) break;
+      }
+      r.d2 = best;
+      r.idx = bidx;
+      return r;
+    }
+  }
   if (inside && reach < (float)(kOffR - 1) * blk) {
     // nearest-first over the sorted offsets; q lies in block cb up to FP32 rounding (4 um slack)
     for (int base = 0; base < kOffN; base += 32) {
@@ -471,6 +548,46 @@ __device__ __forceinline__ bool cloud_outside_warp(const PmPrim& P, const PmGrid
   if (near) *near = nn.idx;
   if (nn.idx < 0) return true;
   return sqrt(nn.d2) - P.a > r;
+}
+
+// Starting candidate of a warp search: the best of the stored nearest points of the 8 fine-cell
+// centres around q (lanes 0-7, one centre each), shared by the warp.  (INFINITY, -1) if none.
+__device__ __forceinline__ NNResult32 field_corner_candidate(const PmGridDev& G, float qx, float qy, float qz) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  float d2 = INFINITY;
+  int idx = -1;
+  if (lane < 8 && G.n_points > 0) {
+    const float inv = (float)(PM_GRID_B / G.block);
+    const float qa[3] = {qx, qy, qz};
+    const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
+    int cc[3];
+    bool ok = true;
+    for (int a = 0; a < 3; a++) {
+      const float t = floorf((qa[a] - (float)G.origin[a]) * inv - 0.5f) + (float)((lane >> a) & 1);
+      ok = ok && t >= 0.f && t <= (float)(nc[a] - 1);
+      cc[a] = ok ? (int)t : 0;
+    }
+    if (ok) {
+      const int2 nn = __ldg(G.cell_nn + cc[0] + nc[0] * (cc[1] + nc[1] * cc[2]));
+      if (nn.y >= 0) {
+        d2 = point_d2_32(G, nn.y, qx, qy, qz);
+        idx = nn.y;
+      }
+    }
+  }
+  unsigned long long key = idx >= 0 ? nn_key(d2, idx) : ~0ull;
+  for (int o = 4; o > 0; o >>= 1) {
+    const unsigned long long k2 = __shfl_xor_sync(FULL, key, o);
+    key = k2 < key ? k2 : key;
+  }
+  key = __shfl_sync(FULL, key, 0);
+  NNResult32 r{INFINITY, -1};
+  if (key != ~0ull) {
+    r.d2 = __uint_as_float((unsigned)(key >> 32));
+    r.idx = (int)(unsigned)(key & 0xffffffffu);
+  }
+  return r;
 }
 
 __device__ __forceinline__ int f2o(float f) {
@@ -748,9 +865,8 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
       const float reach = Pr.a + S.r + (want_dist ? m + cutoff : m);
       const PmGridDev& Gc = v.C[Pr.cloud];
-      const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z);
-      const float d2_0 = fb.idx >= 0 ? point_d2_32(Gc, fb.idx, sc.x, sc.y, sc.z) : INFINITY;
-      const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, d2_0, fb.idx);
+      const NNResult32 start = field_corner_candidate(Gc, sc.x, sc.y, sc.z);
+      const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, start.d2, start.idx);
       if (lane == 0) {
         float g, sd, mag;
         if (nn.idx < 0) {

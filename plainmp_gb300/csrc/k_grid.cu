@@ -3,6 +3,7 @@
 // block-major) -> per-cell counts -> exclusive scan -> scatter -> occupied-cell records with
 // conservative FP32 boxes -> per-block record ranges and boxes.  The order of points inside a
 // cell follows atomic arrival and is not fixed; nearest distances do not depend on it.
+#include <algorithm>
 #include <vector>
 
 #include "pm_grid.cuh"
@@ -238,6 +239,95 @@ __global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int
   out[i] = make_int2(__float_as_int(fmaxf(d * (1.0f - 1e-6f) - slack, 0.0f)), idx);
 }
 
+// Per-block candidate lists.  For a block whose cells all have a nearest point in the field, a
+// query q inside it (up to FP32 rounding of its block) has a point within
+//   ub(q) = |q - p(c)| <= |q - c| + |c - p(c)| <= half cell diagonal + d(c)
+// for its field cell c (inside the block or a neighbour, taken over the block's cells plus a one-cell
+// shell), so the exact search needs only the occupied blocks within R_B = max(d(c)) + 1.5 cell
+// diagonals of the block's box.  Pass 0: R_B and the list length; pass 1 (after a scan): the
+// lists, sorted by box distance.
+__device__ __forceinline__ float box_box_d(const float* a_lo, const float* a_hi, const float* b) {
+  float d2 = 0.f;
+  for (int k = 0; k < 3; k++) {
+    const float g = fmaxf(fmaxf(b[k] - a_hi[k], a_lo[k] - b[3 + k]), 0.f);
+    d2 = fmaf(g, g, d2);
+  }
+  return sqrtf(d2);
+}
+__global__ void k_blk_lists(PmGridDev G, int pass, float reach_cap, float* __restrict__ R, int32_t* __restrict__ cnt,
+                            const int32_t* __restrict__ start, int2* __restrict__ cand) {
+  const int nbx = G.nbx, nby = G.nby, nbz = G.nbz;
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= (int64_t)nbx * nby * nbz) return;
+  const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
+  const float cell = (float)(G.block / PM_GRID_B);
+  float rb;
+  if (pass == 0) {
+    const int nc[3] = {nbx * PM_GRID_B, nby * PM_GRID_B, nbz * PM_GRID_B};
+    float dmax = 0.f;
+    bool ok = true;
+    for (int cz = bz * PM_GRID_B - 1; cz <= (bz + 1) * PM_GRID_B && ok; cz++)
+      for (int cy = by * PM_GRID_B - 1; cy <= (by + 1) * PM_GRID_B && ok; cy++)
+        for (int cx = bx * PM_GRID_B - 1; cx <= (bx + 1) * PM_GRID_B; cx++) {
+          if (cx < 0 || cy < 0 || cz < 0 || cx >= nc[0] || cy >= nc[1] || cz >= nc[2]) continue;
+          const int2 nn = G.cell_nn[cx + (int64_t)nc[0] * (cy + (int64_t)nc[1] * cz)];
+          if (nn.y < 0) {
+            ok = false;
+            break;
+          }
+          // |c - p(c)| with the FP32 expression of the queries' upper bound
+          const float4 p = G.p32[nn.y];
+          const float dx = p.x - field_centre(G.origin[0], cx, cell), dy = p.y - field_centre(G.origin[1], cy, cell),
+                      dz = p.z - field_centre(G.origin[2], cz, cell);
+          dmax = fmaxf(dmax, sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))));
+        }
+    rb = ok ? dmax * 1.00001f + 1.5f * 1.7320508f * cell + 1e-5f : -1.f;
+    if (!(rb <= reach_cap)) rb = -1.f;  // far from the cloud: no list, the walk handles it
+    R[b] = rb;
+  } else {
+    rb = R[b];
+  }
+  if (rb < 0.f) {
+    if (pass == 0) cnt[b] = 0;
+    return;
+  }
+  const float blk = (float)G.block;
+  const float slack = 1e-5f;
+  const float lo[3] = {(float)G.origin[0] + (float)bx * blk - slack, (float)G.origin[1] + (float)by * blk - slack,
+                       (float)G.origin[2] + (float)bz * blk - slack};
+  const float hi[3] = {lo[0] + blk + 2.f * slack, lo[1] + blk + 2.f * slack, lo[2] + blk + 2.f * slack};
+  const int k = (int)ceilf(rb / blk) + 1;
+  int n = 0;
+  const int32_t s0 = pass == 1 ? start[b] : 0;
+  for (int z = max(bz - k, 0); z <= min(bz + k, nbz - 1); z++)
+    for (int y = max(by - k, 0); y <= min(by + k, nby - 1); y++)
+      for (int x = max(bx - k, 0); x <= min(bx + k, nbx - 1); x++) {
+        const int64_t o = x + (int64_t)nbx * (y + (int64_t)nby * z);
+        const int2 occ = reinterpret_cast<const int2*>(G.blk_occ)[o];
+        if (occ.x >= occ.y) continue;
+        const float d = box_box_d(lo, hi, G.blk_box + 6 * o);
+        if (!(d < rb * 1.00001f + 1e-6f)) continue;
+        if (pass == 1) {  // insertion by distance
+          int j = n;
+          while (j > 0) {
+            if (__int_as_float(cand[s0 + j - 1].y) <= d) break;
+            cand[s0 + j] = cand[s0 + j - 1];
+            j--;
+          }
+          cand[s0 + j] = make_int2((int32_t)o, __float_as_int(d));
+        }
+        n++;
+      }
+  if (pass == 0) cnt[b] = n;
+}
+
+__global__ void k_blk_ranges(const float* __restrict__ R, const int32_t* __restrict__ cnt, const int32_t* __restrict__ start, int64_t nb,
+                             int2* __restrict__ out) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  out[b] = R[b] < 0.f ? make_int2(-1, -1) : make_int2(start[b], start[b] + cnt[b]);
+}
+
 inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -254,6 +344,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   g.n_allocs = 0;
   auto keep = [&](size_t bytes, void** p) -> cudaError_t {
+    if (g.n_allocs >= (int)(sizeof(g.allocs) / sizeof(g.allocs[0]))) return cudaErrorMemoryAllocation;
     cudaError_t r = cudaMalloc(p, bytes < 16 ? 16 : bytes);
     if (r == cudaSuccess) g.allocs[g.n_allocs++] = *p;
     return r;
@@ -281,6 +372,10 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   uint8_t* edf = nullptr;
   float* cell_lb = nullptr;
   int2* cell_nn = nullptr;
+  int2* blk_list = nullptr;
+  int2* blk_cand = nullptr;
+  float* blk_reach = nullptr;
+  int32_t n_cand = 0;
   float *blk_box = nullptr, *cell_box = nullptr;
   int32_t n_rec = 0;
   do {
@@ -351,6 +446,9 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       const int64_t ncl = (int64_t)nc[0] * nc[1] * nc[2];
       if ((e = keep(ncl * 8, (void**)&cell_nn)) != cudaSuccess) break;
       PmGridDev v = d;
+      v.blk_list = nullptr;  // the walks below run without candidate lists
+      v.blk_cand = nullptr;
+      v.blk_reach = nullptr;
       v.px = px;
       v.py = py;
       v.pz = pz;
@@ -363,6 +461,25 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       v.cell_lb = cell_lb;
       v.n_points = (int32_t)n;
       k_field<<<nblk(ncl, 128), 128, 0, s>>>(v, nc[0], nc[1], nc[2], (float)g.field_reach, cell_nn);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+      // per-block candidate lists
+      v.cell_nn = cell_nn;
+      int32_t *cnt = nullptr, *lstart = nullptr;
+      if ((e = keep(nblocks * 4, (void**)&blk_reach)) != cudaSuccess) break;
+      if ((e = keep(nblocks * 8, (void**)&blk_list)) != cudaSuccess) break;
+      if ((e = scratch(nblocks * 4, (void**)&cnt)) != cudaSuccess) break;
+      if ((e = scratch(nblocks * 4, (void**)&lstart)) != cudaSuccess) break;
+      k_blk_lists<<<nblk(nblocks, 128), 128, 0, s>>>(v, 0, (float)g.field_reach, blk_reach, cnt, nullptr, nullptr);
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
+      if ((e = exclusive_scan(cnt, nblocks, lstart, s, tmp)) != cudaSuccess) break;
+      int32_t last_start = 0, last_cnt = 0;
+      if ((e = cudaMemcpyAsync(&last_start, lstart + nblocks - 1, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+      if ((e = cudaMemcpyAsync(&last_cnt, cnt + nblocks - 1, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+      n_cand = last_start + last_cnt;
+      if ((e = keep((size_t)std::max<int32_t>(n_cand, 1) * 8, (void**)&blk_cand)) != cudaSuccess) break;
+      k_blk_lists<<<nblk(nblocks, 128), 128, 0, s>>>(v, 1, (float)g.field_reach, blk_reach, cnt, lstart, blk_cand);
+      k_blk_ranges<<<nblk(nblocks, 256), 256, 0, s>>>(blk_reach, cnt, lstart, nblocks, blk_list);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
     e = cudaStreamSynchronize(s);
@@ -383,6 +500,9 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.edf = edf;
   d.cell_lb = cell_lb;
   d.cell_nn = cell_nn;
+  d.blk_list = blk_list;
+  d.blk_cand = blk_cand;
+  d.blk_reach = blk_reach;
   d.field_reach = (float)g.field_reach;
   d.n_points = (int32_t)n;
   return cudaSuccess;

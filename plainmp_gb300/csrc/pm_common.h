@@ -85,6 +85,10 @@ struct PmGridDev {
                            // within field_reach)
   float field_reach;       // cell_nn searched up to this distance from each centre
   int32_t pad_nn;
+  const int2* blk_list;    // per block: [first, end) of its candidate list in blk_cand (first = -1: none)
+  const int2* blk_cand;    // candidate lists: (occupied block, float bits of its box distance from the listing
+                           // block's box), nearest first, within blk_reach
+  const float* blk_reach;  // per block: a query in the block whose search bound is below this needs only its list
   int32_t nbx, nby, nbz;   // blocks per axis
   int32_t n_points;
   double origin[3];        // grid origin (world)

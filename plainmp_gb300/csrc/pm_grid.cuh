@@ -142,6 +142,34 @@ __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float 
     if (!(f >= 0.f && f <= (float)(nb[a] - 1))) inside = false;
     cb[a] = f < 0.f ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
   }
+  if (inside && G.blk_list) {  // the block's candidate list covers every point within its reach
+    const int b = cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]);
+    const int2 rng = __ldg(G.blk_list + b);
+    if (rng.x >= 0 && sqrtf(r.d2) <= __ldg(G.blk_reach + b)) {
+      for (int k = rng.x; k < rng.y; k++) {
+        const int2 e = __ldg(G.blk_cand + k);
+        const float ed = __int_as_float(e.y);
+        if (ed * ed * (1.0f - 1e-5f) >= r.d2) break;  // sorted: no later entry can be closer
+        const int bb = e.x;
+        if (box_d2_32(G.blk_box + 6 * bb, qx, qy, qz) >= r.d2) continue;
+        const int2 occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + bb);
+        for (int c = occ.x; c < occ.y; c++) {
+          if (box_d2_32(G.cell_box + 6 * c, qx, qy, qz) >= r.d2) continue;
+          const int2 pr = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + c);
+          for (int i = pr.x; i < pr.y; i++) {
+            const float4 p = __ldg(G.p32 + i);
+            const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (d2 < r.d2) {
+              r.d2 = d2;
+              r.idx = i;
+            }
+          }
+        }
+      }
+      return r;
+    }
+  }
   const int k0 = __ldg(G.edf + cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]));
   if (inside && k0 >= 2) {
     const float lb0 = (float)(k0 - 1) * blk - 4e-6f;

@@ -87,7 +87,7 @@ struct GridBuild {
   double field_reach = 0.3;  // nearest-point field: search radius around each cell centre
   // outputs (owned by the caller after the call; freed with grid_free)
   PmGridDev dev;
-  void* allocs[16];
+  void* allocs[24];
   int n_allocs;
 };
 // Builds the grid synchronously on `s` (allocates device memory); returns cudaSuccess or the
