@@ -303,10 +303,10 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
   float best = init_d2 < maxd2 ? init_d2 : maxd2;
   int bidx = init_d2 < maxd2 ? init_idx : -1;
   const float reach = sqrtf(maxd2);
-  const float blk = (float)G.block;
-  const float inv = (float)(1.0 / G.block);
+  const float blk = G.blk32;
+  const float inv = G.inv_blk32;
   const float qa[3] = {qx, qy, qz};
-  const float oa[3] = {(float)G.origin[0], (float)G.origin[1], (float)G.origin[2]};
+  const float oa[3] = {G.o32[0], G.o32[1], G.o32[2]};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
   int cb[3];
   bool inside = true;
@@ -558,13 +558,13 @@ __device__ __forceinline__ NNResult32 field_corner_candidate(const PmGridDev& G,
   float d2 = INFINITY;
   int idx = -1;
   if (lane < 8 && G.n_points > 0) {
-    const float inv = (float)(PM_GRID_B / G.block);
+    const float inv = G.inv_cell32;
     const float qa[3] = {qx, qy, qz};
     const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
     int cc[3];
     bool ok = true;
     for (int a = 0; a < 3; a++) {
-      const float t = floorf((qa[a] - (float)G.origin[a]) * inv - 0.5f) + (float)((lane >> a) & 1);
+      const float t = floorf((qa[a] - G.o32[a]) * inv - 0.5f) + (float)((lane >> a) & 1);
       ok = ok && t >= 0.f && t <= (float)(nc[a] - 1);
       cc[a] = ok ? (int)t : 0;
     }
@@ -668,7 +668,7 @@ struct EdgeSource {
     const double* b = s2 + e * d;
     if (k == 0) return b;
     const double r = sr[e];
-    const unsigned long long n_test = (unsigned long long)(floor(1 / r) + 2);
+    const unsigned long long n_test = (unsigned long long)n[e] + 1;  // floor(1 / r) + 2, from k_edge_setup
     double t;
     if (n_test < 129) {
       t = (double)seq[(n_test - 1) * 128 + (k + 1)] * r;
@@ -993,7 +993,7 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
     s.r = (float)v.sr[i];
     s.group = v.sgroup[i];
     s.tiny = v.sr[i] < 1e-6;
-    s.sn = (float)(sqrt(v.sx[i] * v.sx[i] + v.sy[i] * v.sy[i] + v.sz[i] * v.sz[i]) * (1.0 + 1e-6));
+    s.sn = sqrtf(fmaf(s.x, s.x, fmaf(s.y, s.y, s.z * s.z))) * 1.000002f + 1e-9f;  // rounded up
     sm.sph[i] = s;
   }
   for (int i = tid; i < T->n_groups; i += blockDim.x) {
@@ -1008,7 +1008,7 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
     g.count = G.count;
     g.only_self = G.only_self;
     g.tiny = G.radius < 1e-6;
-    g.gn = (float)(sqrt(G.rel[0] * G.rel[0] + G.rel[1] * G.rel[1] + G.rel[2] * G.rel[2]) * (1.0 + 1e-6));
+    g.gn = sqrtf(fmaf(g.rel[0], g.rel[0], fmaf(g.rel[1], g.rel[1], g.rel[2] * g.rel[2]))) * 1.000002f + 1e-9f;
     sm.grp[i] = g;
   }
   for (int i = tid; i < T->n_prims; i += blockDim.x) {

@@ -4,6 +4,7 @@
 // conservative FP32 boxes -> per-block record ranges and boxes.  The order of points inside a
 // cell follows atomic arrival and is not fixed; nearest distances do not depend on it.
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "pm_grid.cuh"
@@ -223,9 +224,8 @@ __global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)ncx * ncy * ncz) return;
   const int cx = (int)(i % ncx), cy = (int)((i / ncx) % ncy), cz = (int)(i / ((int64_t)ncx * ncy));
-  const float cellf = (float)(G.block / PM_GRID_B);
-  const float x = field_centre(G.origin[0], cx, cellf), y = field_centre(G.origin[1], cy, cellf),
-              z = field_centre(G.origin[2], cz, cellf);
+  const float x = field_centre(G.o32[0], cx, G.cell32), y = field_centre(G.o32[1], cy, G.cell32),
+              z = field_centre(G.o32[2], cz, G.cell32);
   const float slack = 4e-6f + 2e-7f * (fabsf(x) + fabsf(y) + fabsf(z));
   float d = reach;
   int idx = -1;
@@ -260,7 +260,7 @@ __global__ void k_blk_lists(PmGridDev G, int pass, float reach_cap, float* __res
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= (int64_t)nbx * nby * nbz) return;
   const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
-  const float cell = (float)(G.block / PM_GRID_B);
+  const float cell = G.cell32;
   float rb;
   if (pass == 0) {
     const int nc[3] = {nbx * PM_GRID_B, nby * PM_GRID_B, nbz * PM_GRID_B};
@@ -277,8 +277,8 @@ __global__ void k_blk_lists(PmGridDev G, int pass, float reach_cap, float* __res
           }
           // |c - p(c)| with the FP32 expression of the queries' upper bound
           const float4 p = G.p32[nn.y];
-          const float dx = p.x - field_centre(G.origin[0], cx, cell), dy = p.y - field_centre(G.origin[1], cy, cell),
-                      dz = p.z - field_centre(G.origin[2], cz, cell);
+          const float dx = p.x - field_centre(G.o32[0], cx, cell), dy = p.y - field_centre(G.o32[1], cy, cell),
+                      dz = p.z - field_centre(G.o32[2], cz, cell);
           dmax = fmaxf(dmax, sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))));
         }
     rb = ok ? dmax * 1.00001f + 1.5f * 1.7320508f * cell + 1e-5f : -1.f;
@@ -291,10 +291,9 @@ __global__ void k_blk_lists(PmGridDev G, int pass, float reach_cap, float* __res
     if (pass == 0) cnt[b] = 0;
     return;
   }
-  const float blk = (float)G.block;
+  const float blk = G.blk32;
   const float slack = 1e-5f;
-  const float lo[3] = {(float)G.origin[0] + (float)bx * blk - slack, (float)G.origin[1] + (float)by * blk - slack,
-                       (float)G.origin[2] + (float)bz * blk - slack};
+  const float lo[3] = {G.o32[0] + (float)bx * blk - slack, G.o32[1] + (float)by * blk - slack, G.o32[2] + (float)bz * blk - slack};
   const float hi[3] = {lo[0] + blk + 2.f * slack, lo[1] + blk + 2.f * slack, lo[2] + blk + 2.f * slack};
   const int k = (int)ceilf(rb / blk) + 1;
   int n = 0;
@@ -329,6 +328,17 @@ __global__ void k_blk_ranges(const float* __restrict__ R, const int32_t* __restr
 }
 
 inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+// FP32 roundings of a double toward -inf / +inf (host)
+inline float round_down_f(double v) {
+  float f = (float)v;
+  if ((double)f > v) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+inline float round_up_f(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = std::nextafter(f, INFINITY);
+  return f;
+}
 
 }  // namespace
 
@@ -361,6 +371,15 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   if (!(d.nbx >= 1 && d.nby >= 1 && d.nbz >= 1 && n >= 0 && g.cell > 0.0 && d.block > 0.0 && g.field_reach > 0.0) ||
       (int64_t)d.nbx * d.nby * d.nbz * PM_GRID_CELLS_PER_BLOCK > ((int64_t)1 << 30))
     return cudaErrorInvalidValue;
+  for (int a = 0; a < 3; a++) {
+    d.o32[a] = (float)d.origin[a];
+    d.box_lo32[a] = round_down_f(d.lb[a] + d.radius);
+    d.box_hi32[a] = round_up_f(d.ub[a] - d.radius);
+  }
+  d.blk32 = (float)d.block;
+  d.inv_blk32 = (float)(1.0 / d.block);
+  d.cell32 = (float)(d.block / PM_GRID_B);
+  d.inv_cell32 = (float)(PM_GRID_B / d.block);
   const int nb[3] = {d.nbx, d.nby, d.nbz};
   const int nc[3] = {nb[0] * PM_GRID_B, nb[1] * PM_GRID_B, nb[2] * PM_GRID_B};
   const int64_t nblocks = (int64_t)nb[0] * nb[1] * nb[2];

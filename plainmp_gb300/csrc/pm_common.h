@@ -89,6 +89,10 @@ struct PmGridDev {
   const int2* blk_cand;    // candidate lists: (occupied block, float bits of its box distance from the listing
                            // block's box), nearest first, within blk_reach
   const float* blk_reach;  // per block: a query in the block whose search bound is below this needs only its list
+  // FP32 copies for the FP32 queries (no FP64 arithmetic on their path): origin, block edge and
+  // its reciprocal, fine cell edge and its reciprocal, and the points' box (rounded outwards)
+  float o32[3], blk32, inv_blk32, cell32, inv_cell32;
+  float box_lo32[3], box_hi32[3];
   int32_t nbx, nby, nbz;   // blocks per axis
   int32_t n_points;
   double origin[3];        // grid origin (world)

@@ -129,9 +129,9 @@ __device__ __forceinline__ float box_d2_32(const float* b, float qx, float qy, f
 __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2 = INFINITY) {
   NNResult32 r{maxd2, -1};
   if (G.n_points <= 0) return r;
-  const float inv = (float)(1.0 / G.block);
-  const float ox = (float)G.origin[0], oy = (float)G.origin[1], oz = (float)G.origin[2];
-  const float blk = (float)G.block;
+  const float inv = G.inv_blk32;
+  const float ox = G.o32[0], oy = G.o32[1], oz = G.o32[2];
+  const float blk = G.blk32;
   const float qa[3] = {qx, qy, qz};
   const float oa[3] = {ox, oy, oz};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
@@ -223,7 +223,7 @@ __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float 
 
 // Centre of fine cell c along one axis.  The build and the queries evaluate this same FP32
 // expression, so a query measures its offset from exactly the point whose distance was stored.
-__device__ __forceinline__ float field_centre(double origin, int c, float cellf) { return (float)origin + ((float)c + 0.5f) * cellf; }
+__device__ __forceinline__ float field_centre(float origin, int c, float cellf) { return origin + ((float)c + 0.5f) * cellf; }
 
 // Nearest-point field of a query q: lb = a lower bound on the distance from q to any point, by the
 // triangle inequality from the distance of a fine-cell centre c (lb = d(c) - |q - c|, any cell
@@ -237,21 +237,21 @@ struct FieldLB {
 __device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, float qy, float qz) {
   FieldLB f{INFINITY, -1};
   if (G.n_points <= 0) return f;
-  const float cellf = (float)(G.block / PM_GRID_B);
-  const float inv = (float)(PM_GRID_B / G.block);
+  const float cellf = G.cell32;
+  const float inv = G.inv_cell32;
   const float qa[3] = {qx, qy, qz};
   const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
   int cc[3];
   bool inside = true;
   for (int a = 0; a < 3; a++) {
-    const float t = floorf((qa[a] - (float)G.origin[a]) * inv);
+    const float t = floorf((qa[a] - G.o32[a]) * inv);
     if (!(t >= 0.f && t <= (float)(nc[a] - 1))) inside = false;
     cc[a] = inside ? (int)t : 0;
   }
   if (!inside) {
     float d2 = 0.f;
     for (int a = 0; a < 3; a++) {
-      const float lo = __double2float_rd(G.lb[a] + G.radius), hi = __double2float_ru(G.ub[a] - G.radius);
+      const float lo = G.box_lo32[a], hi = G.box_hi32[a];
       const float gap = fmaxf(fmaxf(lo - qa[a], qa[a] - hi), 0.f);
       d2 = fmaf(gap, gap, d2);
     }
@@ -259,8 +259,8 @@ __device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, fl
     return f;
   }
   const int2 nn = __ldg(G.cell_nn + cc[0] + nc[0] * (cc[1] + nc[1] * cc[2]));
-  const float dx = qx - field_centre(G.origin[0], cc[0], cellf), dy = qy - field_centre(G.origin[1], cc[1], cellf),
-              dz = qz - field_centre(G.origin[2], cc[2], cellf);
+  const float dx = qx - field_centre(G.o32[0], cc[0], cellf), dy = qy - field_centre(G.o32[1], cc[1], cellf),
+              dz = qz - field_centre(G.o32[2], cc[2], cellf);
   const float off = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * (1.0f + 1e-6f) + 1e-7f;
   f.lb = fmaxf(__int_as_float(nn.x) - off, 0.f);
   f.idx = nn.y;
@@ -278,9 +278,9 @@ __device__ __forceinline__ float point_d2_32(const PmGridDev& G, int idx, float 
 // block distance field alone: 0 when q is outside the grid or near an occupied block.
 __device__ __forceinline__ float grid_lower_bound32(const PmGridDev& G, float qx, float qy, float qz) {
   if (G.n_points <= 0) return INFINITY;
-  const float inv = (float)(1.0 / G.block);
+  const float inv = G.inv_blk32;
   const float qa[3] = {qx, qy, qz};
-  const float oa[3] = {(float)G.origin[0], (float)G.origin[1], (float)G.origin[2]};
+  const float oa[3] = {G.o32[0], G.o32[1], G.o32[2]};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
   int cb[3];
   for (int a = 0; a < 3; a++) {
@@ -289,7 +289,7 @@ __device__ __forceinline__ float grid_lower_bound32(const PmGridDev& G, float qx
     cb[a] = (int)f;
   }
   const int k0 = __ldg(G.edf + cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]));
-  return k0 >= 2 ? fmaxf((float)(k0 - 1) * (float)G.block - 4e-6f, 0.f) : 0.f;
+  return k0 >= 2 ? fmaxf((float)(k0 - 1) * G.blk32 - 4e-6f, 0.f) : 0.f;
 }
 
 // Lower bound on the distance from q to any point: inside the grid, the Euclidean distance from
@@ -298,9 +298,9 @@ __device__ __forceinline__ float grid_lower_bound32(const PmGridDev& G, float qx
 // covers the FP32 cell assignment of q.
 __device__ __forceinline__ float grid_cell_lower_bound32(const PmGridDev& G, float qx, float qy, float qz) {
   if (G.n_points <= 0) return INFINITY;
-  const float inv = (float)(PM_GRID_B / G.block);
+  const float inv = G.inv_cell32;
   const float qa[3] = {qx, qy, qz};
-  const float oa[3] = {(float)G.origin[0], (float)G.origin[1], (float)G.origin[2]};
+  const float oa[3] = {G.o32[0], G.o32[1], G.o32[2]};
   const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
   int cc[3];
   bool inside = true;
@@ -312,7 +312,7 @@ __device__ __forceinline__ float grid_cell_lower_bound32(const PmGridDev& G, flo
   if (!inside) {
     float d2 = 0.f;
     for (int a = 0; a < 3; a++) {
-      const float lo = __double2float_rd(G.lb[a] + G.radius), hi = __double2float_ru(G.ub[a] - G.radius);
+      const float lo = G.box_lo32[a], hi = G.box_hi32[a];
       const float gap = fmaxf(fmaxf(lo - qa[a], qa[a] - hi), 0.f);
       d2 = fmaf(gap, gap, d2);
     }
