@@ -211,6 +211,31 @@ int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t
 int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type,
                             const double* width, double resolution, uint8_t* out, int64_t* stats, int mem, void* stream);
 
+/* ---------------------------------------------------------------- pose constraints
+ * LinkPoseCst(kin, control_joints, base_type, link_names, poses) (constraints/primitive_link_pose.cpp:
+ * 16-71; bindings/constraint.cpp:46-53): one target per link, pose_dims[i] = 3 (position), 6
+ * (position + RPY) or 7 (position + quaternion x y z w), targets concatenated in `poses`.  Other
+ * dimensions give PMGPU_ERR_RUNTIME ("All poses must be 3 or 6 or 7 dimensional").
+ * LinkPositionBoundCst(kin, control_joints, base_type, link, axis, lb, ub) (constraints/
+ * primitive_link_position_bound.cpp:15-83; bindings/constraint.cpp:98-103): an absent bound has
+ * has_lb / has_ub = 0; axis > 2 or no bound give PMGPU_ERR_RUNTIME.
+ * Both share one handle type; the model is shared like the reference's KinematicModel. */
+typedef struct pmgpu_posecst pmgpu_posecst;
+int pmgpu_linkpose_create(pmgpu_model* kin, const char* const* control_joints, int n_joints, int base_type, const char* const* links,
+                          int n_links, const double* poses, const int32_t* pose_dims, pmgpu_posecst** out);
+int pmgpu_linkbound_create(pmgpu_model* kin, const char* const* control_joints, int n_joints, int base_type, const char* link, int axis,
+                           int has_lb, double lb, int has_ub, double ub, pmgpu_posecst** out);
+void pmgpu_posecst_destroy(pmgpu_posecst* c);
+/* q_dim, cst_dim and whether the constraint is an equality (LinkPoseCst) */
+int pmgpu_posecst_dims(const pmgpu_posecst* c, int* q_dim, int* cst_dim, int* is_equality);
+/* ConstraintBase::evaluate(q) (constraints/primitive.hpp:74-79) for B configurations, FP64:
+ * vals B x cst_dim, jac B x cst_dim x q_dim (row-major), either may be NULL.  The rows follow
+ * get_jacobian (kinematics/algorithm.cpp:212-344) with RotationType IGNORE / RPY / XYZW. */
+int pmgpu_posecst_evaluate(pmgpu_posecst* c, const double* q, int64_t B, double* vals, double* jac, int mem, void* stream);
+/* IneqConstraintBase::is_valid(q) of a LinkPositionBoundCst (update_kintree(q, false) +
+ * is_valid_dirty); an equality constraint gives PMGPU_ERR_INVALID. */
+int pmgpu_posecst_is_valid(pmgpu_posecst* c, const double* q, int64_t B, uint8_t* out, int mem, void* stream);
+
 /* ---------------------------------------------------------------- link poses
  * World pose (x y z qx qy qz qw) of `link` for B configurations, FP64, the FK of
  * ConstraintBase::update_kintree with std::sin/std::cos (constraints/primitive.hpp:38-62)

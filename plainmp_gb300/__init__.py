@@ -7,7 +7,8 @@ modules mirror the reference's ``plainmp.kinematics``, ``plainmp.psdf`` and
 ``plainmp.constraint`` interfaces.
 """
 from ._lib import CudaError, DeviceTimeout, device_count  # noqa: F401
-from .constraint import SphereAttachmentSpec, SphereCollisionCst  # noqa: F401
+from .constraint import (EqCompositeCst, IneqCompositeCst, LinkPoseCst, LinkPositionBoundCst,  # noqa: F401
+                         SphereAttachmentSpec, SphereCollisionCst)
 from .kinematics import BaseType, KinematicModel  # noqa: F401
 from .motion_validator import BoxMotionValidator, EuclideanMotionValidator  # noqa: F401
 from .psdf import BoxSDF, CloudSDF, CylinderSDF, GroundSDF, Pose, SDFBase, SphereSDF, UnionSDF  # noqa: F401

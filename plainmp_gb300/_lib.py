@@ -104,6 +104,12 @@ _SIGS = {
     "pmgpu_cst_set_fast_launch": (_i, [_p, _i, _i]),
     "pmgpu_cst_get_fast_launch": (_i, [_p, C.POINTER(_i), C.POINTER(_i)]),
     "pmgpu_cst_link_poses": (_i, [_p, C.c_int32, _p, _i64, _p, _i, _p]),
+    "pmgpu_linkpose_create": (_i, [_p, _cpp, _i, _i, _cpp, _i, _dp, _i32p, C.POINTER(_p)]),
+    "pmgpu_linkbound_create": (_i, [_p, _cpp, _i, _i, C.c_char_p, _i, _i, _d, _i, _d, C.POINTER(_p)]),
+    "pmgpu_posecst_destroy": (None, [_p]),
+    "pmgpu_posecst_dims": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    "pmgpu_posecst_evaluate": (_i, [_p, _p, _i64, _p, _p, _i, _p]),
+    "pmgpu_posecst_is_valid": (_i, [_p, _p, _i64, _p, _i, _p]),
     "pmgpu_ik_cost": (_i, [_p, _p, _p, _p, _i64, _p, _p, _i, _p]),
     "pmgpu_ik_descend": (_i, [_p, _p, _p, _p, _i64, C.c_int32, C.c_float, C.c_int32, _p, _p, _i, _p]),
     "pmgpu_traj_cost": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p, _i, _p]),

@@ -206,3 +206,174 @@ class SphereCollisionCst:
         if stats:
             res.append({"configs": int(st[0]), "rechecked_terms": int(st[1]), "rechecked_configs": int(st[2])})
         return res[0] if len(res) == 1 else tuple(res)
+
+
+# ------------------------------------------------------------------ pose constraints, composites
+class _PoseCstBase:
+    """Shared part of LinkPoseCst / LinkPositionBoundCst (one C handle type, pmgpu_posecst)."""
+
+    def __init__(self, kin: KinematicModel, control_joint_names: Sequence[str], base_type: BaseType):
+        self._kin = kin
+        self.control_joint_names = list(control_joint_names)
+        self.base_type = BaseType(int(base_type))
+        self._h = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.pmgpu_posecst_destroy(h)
+            self._h = None
+
+    def _dims(self):
+        qd, cd, eq = C.c_int(), C.c_int(), C.c_int()
+        check(lib.pmgpu_posecst_dims(self._h, C.byref(qd), C.byref(cd), C.byref(eq)))
+        return qd.value, cd.value, bool(eq.value)
+
+    def q_dim(self) -> int:
+        return self._dims()[0]
+
+    def cst_dim(self) -> int:
+        return self._dims()[1]
+
+    def get_kin(self) -> KinematicModel:
+        return self._kin
+
+    def get_control_joint_names(self) -> List[str]:
+        return list(self.control_joint_names)
+
+    def _batch(self, Q):
+        b = Batch(Q)
+        if len(b.shape) != 2 or b.shape[1] != self.q_dim():
+            raise ValueError(f"expected a (B, {self.q_dim()}) batch, got {b.shape}")
+        return b
+
+    def evaluate_batch(self, Q):
+        """ConstraintBase.evaluate for every row of Q: (vals (B, cst_dim), jac (B, cst_dim, q_dim)), FP64."""
+        b = self._batch(Q)
+        m, d = self.cst_dim(), self.q_dim()
+        vals, vp = b.empty((b.shape[0], m), np.float64)
+        jac, jp = b.empty((b.shape[0], m, d), np.float64)
+        check(lib.pmgpu_posecst_evaluate(self._h, b.ptr, b.shape[0], vp, jp, b.mem, b.stream))
+        return vals, jac
+
+    def evaluate(self, q) -> Tuple[np.ndarray, np.ndarray]:
+        qq = f64(q, (1, self.q_dim()))
+        vals, jac = self.evaluate_batch(qq)
+        return vals[0], jac[0]
+
+
+class LinkPoseCst(_PoseCstBase):
+    """LinkPoseCst(kin, control_joint_names, base_type, link_names, poses): poses of 3 (position),
+    6 (position + RPY) or 7 (position + quaternion xyzw) values (constraints/primitive_link_pose.cpp)."""
+
+    def __init__(self, kin: KinematicModel, control_joint_names: Sequence[str], base_type: BaseType, link_names: Sequence[str],
+                 poses: Sequence[np.ndarray]):
+        super().__init__(kin, control_joint_names, base_type)
+        if len(link_names) != len(poses):
+            raise ValueError("one pose per link")
+        self._poses = [f64(p).reshape(-1) for p in poses]
+        dims = np.array([p.shape[0] for p in self._poses], dtype=np.int32)
+        flat = np.ascontiguousarray(np.concatenate(self._poses) if self._poses else np.zeros(1))
+        h = C.c_void_p()
+        check(lib.pmgpu_linkpose_create(kin._h, cstrs(self.control_joint_names), len(self.control_joint_names), int(self.base_type),
+                                        cstrs(list(link_names)), len(link_names), dptr(flat),
+                                        dims.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(h)))
+        self._h = h
+
+    def get_desired_poses(self) -> List[np.ndarray]:
+        return [p.copy() for p in self._poses]
+
+
+class LinkPositionBoundCst(_PoseCstBase):
+    """LinkPositionBoundCst(kin, control_joint_names, base_type, link_name, axis, lb, ub): lb <= p[axis] <= ub
+    for the link's world position, either bound optional (constraints/primitive_link_position_bound.cpp)."""
+
+    def __init__(self, kin: KinematicModel, control_joint_names: Sequence[str], base_type: BaseType, link_name: str, axis: int,
+                 lb: Optional[float] = None, ub: Optional[float] = None):
+        super().__init__(kin, control_joint_names, base_type)
+        h = C.c_void_p()
+        check(lib.pmgpu_linkbound_create(kin._h, cstrs(self.control_joint_names), len(self.control_joint_names), int(self.base_type),
+                                         link_name.encode(), int(axis), int(lb is not None), float(lb or 0.0), int(ub is not None),
+                                         float(ub or 0.0), C.byref(h)))
+        self._h = h
+
+    def is_valid_batch(self, Q):
+        """(B,) uint8: the link position within the bounds after update_kintree(q, False)."""
+        b = self._batch(Q)
+        out, optr = b.empty((b.shape[0],), np.uint8)
+        check(lib.pmgpu_posecst_is_valid(self._h, b.ptr, b.shape[0], optr, b.mem, b.stream))
+        return out
+
+    def is_valid(self, q) -> bool:
+        return bool(self.is_valid_batch(f64(q, (1, self.q_dim())))[0])
+
+
+class _CompositeBase:
+    """CompositeConstraintBase (constraints/composite_constraint.hpp:21-86): constraints on one
+    kinematic model.  The batched calls evaluate each member on the same batch and stack the rows.
+    The reference drives the shared model with the first member's q mapping; the batched path
+    requires every member to have the same control joints and base type, so the mappings agree."""
+
+    def __init__(self, constraints):
+        self.constraints = list(constraints)
+        if not self.constraints:
+            raise ValueError("a composite constraint needs at least one constraint")
+        k0 = self.constraints[0].get_kin()
+        for c in self.constraints:
+            if c.get_kin() is not k0:
+                raise RuntimeError("All constraints must have the same kinematic chain")
+            if (c.get_control_joint_names() != self.constraints[0].get_control_joint_names()
+                    or c.base_type != self.constraints[0].base_type):
+                raise ValueError("batched composite constraints need the same control joints and base type")
+
+    def q_dim(self) -> int:
+        return self.constraints[0].q_dim()
+
+    def cst_dim(self) -> int:
+        return sum(c.cst_dim() for c in self.constraints)
+
+    def evaluate_batch(self, Q):
+        """(vals (B, cst_dim), jac (B, cst_dim, q_dim)): the members' rows stacked in order."""
+        parts = [c.evaluate_batch(Q) for c in self.constraints]
+        if _is_torch(parts[0][0]):
+            import torch
+
+            return torch.cat([p[0] for p in parts], dim=1), torch.cat([p[1] for p in parts], dim=1)
+        return np.concatenate([p[0] for p in parts], axis=1), np.concatenate([p[1] for p in parts], axis=1)
+
+    def evaluate(self, q):
+        vals, jac = self.evaluate_batch(f64(q, (1, self.q_dim())))
+        return vals[0], jac[0]
+
+    def __str__(self) -> str:
+        lines = ["Composite constraint:", f"total dim: {self.cst_dim()}"]
+        lines += [f"  - {type(c).__name__}: {c.cst_dim()}" for c in self.constraints]
+        return "\n".join(lines) + "\n"
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+class EqCompositeCst(_CompositeBase):
+    """EqCompositeCst(constraints) of equality constraints (LinkPoseCst)."""
+
+
+class IneqCompositeCst(_CompositeBase):
+    """IneqCompositeCst(constraints): is_valid = AND over the members after update_kintree(q, False)
+    (composite_constraint.hpp:98-105)."""
+
+    def is_valid_batch(self, Q, fast: bool = True):
+        """(B,) uint8 AND of the members' validity; SphereCollisionCst members use the FP32 +
+        FP64-recheck path when fast (same booleans), else the plain FP64 method."""
+        ok = None
+        for c in self.constraints:
+            if isinstance(c, SphereCollisionCst):
+                r = c.is_valid_fast(Q) if fast else c.is_valid_batch(Q)
+            else:
+                r = c.is_valid_batch(Q)
+            ok = r if ok is None else (ok & r)
+        return ok
+
+    def is_valid(self, q) -> bool:
+        return bool(self.is_valid_batch(f64(q, (1, self.q_dim())))[0])

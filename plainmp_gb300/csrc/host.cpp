@@ -1939,6 +1939,175 @@ int pmgpu_traj_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, co
   });
 }
 
+// ------------------------------------------------------------------ pose constraints
+}  // extern "C"
+struct pmgpu_posecst {
+  HostCst c;  // kinematic slots of the constrained links (no spheres)
+  std::vector<PmPoseTerm> terms;
+  std::vector<int> links;
+  DevBuf d_terms;
+  uint64_t terms_sig = ~0ull;  // slot numbering the device terms were written with
+  int cst_dim = 0;
+  bool equality = true;
+  const PmPoseTerm* device_terms() {
+    c.tables();
+    uint64_t sig = 0;
+    for (size_t i = 0; i < terms.size(); i++) {
+      terms[i].slot = c.slot_for_link(links[i]);
+      sig = sig * 1315423911ull + (uint64_t)terms[i].slot + 1;
+    }
+    if (!d_terms.p || sig != terms_sig) {
+      d_terms.release();
+      d_terms.ensure(std::max<size_t>(terms.size(), 1) * sizeof(PmPoseTerm));
+      if (!terms.empty())
+        cuda_check(cudaMemcpy(d_terms.p, terms.data(), terms.size() * sizeof(PmPoseTerm), cudaMemcpyHostToDevice), "terms upload");
+      terms_sig = sig;
+    }
+    return d_terms.as<PmPoseTerm>();
+  }
+};
+namespace {
+void posecst_init(pmgpu_posecst* h, pmgpu_model* kin, const char* const* control_joints, int n_joints, int base_type) {
+  check_ptr(kin, "kin");
+  if (base_type < 0 || base_type > 2) throw std::invalid_argument("unknown base type");
+  HostCst& c = h->c;
+  c.kin = kin->m;
+  for (int i = 0; i < n_joints; i++) {  // ConstraintBase ctor -> get_joint_ids (primitive.hpp:30-36)
+    auto it = c.kin->joint_id.find(control_joints[i]);
+    if (it == c.kin->joint_id.end()) throw std::invalid_argument(std::string("no joint named ") + control_joints[i]);
+    c.ids.push_back(it->second);
+  }
+  c.base_type = base_type;
+}
+int link_of(const HostModel& M, const char* name) {
+  auto it = M.link_id.find(name);
+  if (it == M.link_id.end()) throw std::invalid_argument(std::string("no link named ") + name);
+  return it->second;
+}
+}  // namespace
+extern "C" {
+
+int pmgpu_linkpose_create(pmgpu_model* kin, const char* const* control_joints, int n_joints, int base_type, const char* const* links,
+                          int n_links, const double* poses, const int32_t* pose_dims, pmgpu_posecst** out) {
+  return guarded([&] {
+    auto* h = new pmgpu_posecst();
+    try {
+      posecst_init(h, kin, control_joints, n_joints, base_type);
+      size_t off = 0;
+      for (int i = 0; i < n_links; i++) {  // primitive_link_pose.cpp:16-29
+        const int d = pose_dims[i];
+        if (d != 3 && d != 6 && d != 7) fail(PMGPU_ERR_RUNTIME, "All poses must be 3 or 6 or 7 dimensional");
+        PmPoseTerm t;
+        std::memset(&t, 0, sizeof(t));
+        t.kind = PM_TERM_LINK_POSE;
+        t.dim = d;
+        for (int k = 0; k < d; k++) t.target[k] = poses[off + k];
+        off += d;
+        h->links.push_back(link_of(*h->c.kin, links[i]));
+        h->terms.push_back(t);
+        h->cst_dim += d;
+      }
+      h->equality = true;
+      *out = h;
+    } catch (...) {
+      delete h;
+      throw;
+    }
+  });
+}
+
+int pmgpu_linkbound_create(pmgpu_model* kin, const char* const* control_joints, int n_joints, int base_type, const char* link, int axis,
+                           int has_lb, double lb, int has_ub, double ub, pmgpu_posecst** out) {
+  return guarded([&] {
+    auto* h = new pmgpu_posecst();
+    try {
+      posecst_init(h, kin, control_joints, n_joints, base_type);
+      // primitive_link_position_bound.cpp:15-32
+      if (axis < 0 || axis > 2) fail(PMGPU_ERR_RUNTIME, "Axis index must be 0 (x), 1 (y), or 2 (z).");
+      if (!has_lb && !has_ub) fail(PMGPU_ERR_RUNTIME, "At least one of lower or upper bound must be provided.");
+      PmPoseTerm t;
+      std::memset(&t, 0, sizeof(t));
+      t.kind = PM_TERM_POSITION_BOUND;
+      t.axis = axis;
+      t.has_lb = has_lb != 0;
+      t.has_ub = has_ub != 0;
+      t.lb = lb;
+      t.ub = ub;
+      t.dim = t.has_lb + t.has_ub;
+      h->links.push_back(link_of(*h->c.kin, link));
+      h->terms.push_back(t);
+      h->cst_dim = t.dim;
+      h->equality = false;
+      *out = h;
+    } catch (...) {
+      delete h;
+      throw;
+    }
+  });
+}
+
+void pmgpu_posecst_destroy(pmgpu_posecst* c) { delete c; }
+
+int pmgpu_posecst_dims(const pmgpu_posecst* c, int* q_dim, int* cst_dim, int* is_equality) {
+  return guarded([&] {
+    check_ptr(c, "constraint");
+    if (q_dim) *q_dim = c->c.q_dim();
+    if (cst_dim) *cst_dim = c->cst_dim;
+    if (is_equality) *is_equality = c->equality ? 1 : 0;
+  });
+}
+
+int pmgpu_posecst_evaluate(pmgpu_posecst* c, const double* q, int64_t B, double* vals, double* jac, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "constraint");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    const PmPoseTerm* dt = c->device_terms();
+    const PmTablesHdr* T = c->c.tables();
+    const double* st = c->c.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const int d = c->c.q_dim(), m = c->cst_dim;
+    const double* dq = q;
+    double* dv = vals;
+    double* dj = jac;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(c->c.w_in, q, (size_t)B * d, s);
+      if (vals) dv = (double*)c->c.w_out.ensure(std::max<size_t>((size_t)B * m * 8, 16));
+      if (jac) dj = (double*)c->c.w_out2.ensure(std::max<size_t>((size_t)B * m * d * 8, 16));
+    }
+    cuda_check(launch_posecst_eval64(T, st, dt, (int)c->terms.size(), m, dq, B, dv, dj, s), "pose constraint evaluate");
+    if (mem == PMGPU_MEM_HOST) {
+      if (vals) stage_out(vals, dv, (size_t)B * m, s);
+      if (jac) stage_out(jac, dj, (size_t)B * m * d, s);
+      cuda_check(cudaStreamSynchronize(s), "pose constraint evaluate");
+    }
+  });
+}
+
+int pmgpu_posecst_is_valid(pmgpu_posecst* c, const double* q, int64_t B, uint8_t* out, int mem, void* stream) {
+  return guarded([&] {
+    check_ptr(c, "constraint");
+    check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
+    if (c->equality) fail(PMGPU_ERR_INVALID, "an equality constraint has no is_valid");
+    const PmPoseTerm* dt = c->device_terms();
+    const PmTablesHdr* T = c->c.tables();
+    const double* st = c->c.kin->d_state.as<double>();
+    cudaStream_t s = as_stream(stream);
+    const double* dq = q;
+    uint8_t* dout = out;
+    if (mem == PMGPU_MEM_HOST) {
+      dq = stage_in(c->c.w_in, q, (size_t)B * c->c.q_dim(), s);
+      dout = (uint8_t*)c->c.w_out.ensure(std::max<size_t>((size_t)B, 16));
+    }
+    cuda_check(launch_posecst_valid64(T, st, dt, (int)c->terms.size(), dq, B, dout, s), "pose constraint is_valid");
+    if (mem == PMGPU_MEM_HOST) {
+      stage_out(out, dout, (size_t)B, s);
+      cuda_check(cudaStreamSynchronize(s), "pose constraint is_valid");
+    }
+  });
+}
+
 int pmgpu_profile_enable(int on) {
   return guarded([&] { g_prof_enabled = on != 0; });
 }

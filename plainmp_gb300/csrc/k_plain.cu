@@ -16,47 +16,6 @@ __global__ void k_is_valid64(const PmTablesHdr* __restrict__ T, const double* __
   out[b] = is_valid_cfg(v, state, q + b * T->q_dim) ? 1 : 0;
 }
 
-// ------------------------------------------------------------------ transforms for jacobians
-__device__ __forceinline__ DPose pose_inverse(const DPose& a) {  // transform.hpp:88-91
-  double n2 = (a.q.x * a.q.x + a.q.y * a.q.y) + (a.q.z * a.q.z + a.q.w * a.q.w);
-  DQ qi;
-  if (n2 > 0) {
-    qi = DQ{-a.q.x / n2, -a.q.y / n2, -a.q.z / n2, a.q.w / n2};
-  } else {
-    qi = DQ{0, 0, 0, 0};
-  }
-  DPose r;
-  r.q = qi;
-  r.t = qrot(qi, D3{-a.t.x, -a.t.y, -a.t.z});
-  return r;
-}
-__device__ __forceinline__ DPose pose_mul(const DPose& a, const DPose& b) {  // transform.hpp:56-62 (b not identity-flagged)
-  DPose r;
-  r.q = qmul(a.q, b.q);
-  r.t = add(a.t, qrot(a.q, b.t));
-  return r;
-}
-__device__ __forceinline__ D3 get_rpy(const DQ& q) {  // transform.hpp:93-120
-  double sqx = q.x * q.x, sqy = q.y * q.y, sqz = q.z * q.z, sqw = q.w * q.w;
-  double sarg = -2 * (q.x * q.z - q.w * q.y);
-  const double pi_2 = 1.57079632679489661923;
-  double roll, pitch, yaw;
-  if (sarg <= -0.99999) {
-    pitch = -pi_2;
-    roll = 0;
-    yaw = -2 * atan2(q.x, q.y);
-  } else if (sarg >= 0.99999) {
-    pitch = pi_2;
-    roll = 0;
-    yaw = 2 * atan2(q.x, q.y);
-  } else {
-    pitch = asin(sarg);
-    roll = atan2(2 * (q.y * q.z + q.w * q.x), sqw - sqx - sqy + sqz);
-    yaw = atan2(2 * (q.x * q.y + q.w * q.z), sqw + sqx - sqy - sqz);
-  }
-  return D3{roll, pitch, yaw};
-}
-
 // get_attached_point_jacobian (algorithm.cpp:346-433); column c of the 3 x dof jacobian is
 // written to jac[3*c .. 3*c+2]
 __device__ void attached_jacobian(const TView& v, const DPose* pose, int plink_slot, const D3& p, double* jac) {

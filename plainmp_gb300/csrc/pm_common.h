@@ -101,6 +101,19 @@ struct PmGridDev {
   double radius;
 };
 
+// One term of a pose constraint: LinkPoseCst target of one link (constraints/primitive_link_pose.cpp:
+// 31-60; dim 3, 6 or 7) or LinkPositionBoundCst (primitive_link_position_bound.cpp:34-79).
+enum { PM_TERM_LINK_POSE = 0, PM_TERM_POSITION_BOUND = 1 };
+struct PmPoseTerm {
+  int32_t kind;
+  int32_t slot;   // FK slot of the link
+  int32_t dim;    // rows of this term: 3 / 6 / 7 (pose) or 1 / 2 (bound)
+  int32_t axis;   // bound: 0 x, 1 y, 2 z
+  int32_t has_lb, has_ub, pad0, pad1;
+  double target[7];
+  double lb, ub;
+};
+
 struct PmTablesHdr {
   int32_t n_slots, n_ctrl, n_groups, n_spheres;
   int32_t n_pairs, n_prims, q_dim, base_type;

@@ -71,6 +71,12 @@ cudaError_t launch_traj_cost(const PmTablesHdr* T, const PmTablesHdr& h, const d
 cudaError_t launch_link_pose64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int slot, double* out7,
                                cudaStream_t s);
 
+// ---- pose constraints (k_pose.cu): LinkPoseCst / LinkPositionBoundCst terms
+cudaError_t launch_posecst_eval64(const PmTablesHdr* T, const double* state, const PmPoseTerm* terms, int n_terms, int cst_dim,
+                                  const double* q, int64_t B, double* vals, double* jac, cudaStream_t s);
+cudaError_t launch_posecst_valid64(const PmTablesHdr* T, const double* state, const PmPoseTerm* terms, int n_terms, const double* q,
+                                   int64_t B, uint8_t* out, cudaStream_t s);
+
 // ---- SDF utilities (k_plain.cu): prims/clouds describe one SDF (a union is flattened)
 cudaError_t launch_sdf_points(const PmPrim* prims, int n_prims, const PmGridDev* clouds, int is_union, const double* pts,
                               const double* radii, int64_t n, double* eval_out, uint8_t* outside_out, cudaStream_t s);

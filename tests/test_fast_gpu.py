@@ -144,14 +144,19 @@ def test_fast_cloud_near_boundary(oracle, cloud_radius):
     assert rechecked > 0
 
 
-def test_fast_mobile_base(oracle):
+@pytest.mark.parametrize("base,nb", [("PLANAR", 3), ("FLOATING", 6)])
+def test_fast_mobile_base(oracle, base, nb):
     r = W.chain7_robot()
-    r = W.Robot(r.urdf, r.control_joints, r.end_link, r.spheres, r.self_pairs, base_type="PLANAR")
+    r = W.Robot(r.urdf, r.control_joints, r.end_link, r.spheres, r.self_pairs, base_type=base)
     s = W.chain7_scene()
     (_, cst, _), (_, oc, _) = scenes.make_constraint(r, s), oracle.make_constraint(r, s)
     rng = np.random.default_rng(2)
-    Q = np.concatenate([W.chain7_configs(1024, seed=2), rng.normal(0, 0.3, (1024, 3))], axis=1)
-    assert np.array_equal(cst.is_valid_fast(Q), oc.is_valid(Q, threads=8))
+    Q = np.concatenate([W.chain7_configs(1024, seed=2), rng.normal(0, 0.3, (1024, nb))], axis=1)
+    Q[:8, 7:] *= 100.0  # far-away base coordinates and large angles: the FK bound grows with them
+    ref = oc.is_valid(Q, threads=8)
+    assert np.array_equal(cst.is_valid_fast(Q), ref)
+    ok, d32 = cst.is_valid_fast(Q[8:], distances=True)
+    assert np.array_equal(ok, ref[8:])
 
 
 def test_fast_edges_match_oracle(chain):

@@ -188,3 +188,40 @@ def test_batch_calls_fail_loudly_without_gpu():
     kin, cst, _ = scenes.make_constraint(W.chain7_robot(), W.chain7_scene())
     with pytest.raises(CudaError):
         cst.is_valid_batch(W.chain7_configs(4))
+
+
+def test_pose_constraint_construction():
+    """LinkPoseCst / LinkPositionBoundCst / composites: dimensions and the reference's errors
+    (primitive_link_pose.cpp:16-29, primitive_link_position_bound.cpp:15-32,
+    composite_constraint.hpp:24-32); construction is host work."""
+    from plainmp_gb300 import (BaseType, IneqCompositeCst, KinematicModel, LinkPoseCst, LinkPositionBoundCst,
+                               SphereCollisionCst)
+    from plainmp_gb300 import workloads as W
+
+    robot = W.chain7_robot()
+    kin = KinematicModel(robot.urdf)
+    j = robot.control_joints
+    c = LinkPoseCst(kin, j, BaseType.FIXED, [robot.end_link, "link3"], [np.zeros(3), np.zeros(7)])
+    assert c.cst_dim() == 10 and c.q_dim() == 7
+    assert [p.shape[0] for p in c.get_desired_poses()] == [3, 7]
+    assert LinkPoseCst(kin, j, BaseType.PLANAR, ["link2"], [np.zeros(6)]).q_dim() == 10
+    assert LinkPoseCst(kin, j, BaseType.FLOATING, ["link2"], [np.zeros(6)]).q_dim() == 13
+    with pytest.raises(RuntimeError, match="3 or 6 or 7"):
+        LinkPoseCst(kin, j, BaseType.FIXED, ["link2"], [np.zeros(5)])
+    with pytest.raises(ValueError):
+        LinkPoseCst(kin, j, BaseType.FIXED, ["nolink"], [np.zeros(3)])
+    b = LinkPositionBoundCst(kin, j, BaseType.FIXED, robot.end_link, 2, lb=0.1)
+    assert b.cst_dim() == 1
+    assert LinkPositionBoundCst(kin, j, BaseType.FIXED, robot.end_link, 0, lb=-1.0, ub=1.0).cst_dim() == 2
+    with pytest.raises(RuntimeError, match="Axis index"):
+        LinkPositionBoundCst(kin, j, BaseType.FIXED, robot.end_link, 3, lb=0.0)
+    with pytest.raises(RuntimeError, match="At least one"):
+        LinkPositionBoundCst(kin, j, BaseType.FIXED, robot.end_link, 1)
+    specs = _specs(robot)
+    sc = SphereCollisionCst(kin, j, BaseType.FIXED, specs, [], None, True)
+    comp = IneqCompositeCst([sc, b])
+    assert comp.cst_dim() == sc.cst_dim() + 1 and comp.q_dim() == 7
+    assert "LinkPositionBoundCst: 1" in str(comp)
+    other = KinematicModel(robot.urdf)
+    with pytest.raises(RuntimeError, match="same kinematic chain"):
+        IneqCompositeCst([sc, LinkPositionBoundCst(other, j, BaseType.FIXED, robot.end_link, 2, lb=0.1)])
