@@ -183,23 +183,36 @@ def bench_chain7(dev, timed):
 
     robot, scene = W.chain7_robot(), W.chain7_scene()
     _, cst, _ = scenes.make_constraint(robot, scene)
+    from plainmp_gb300 import autotune
+
     Q = torch.tensor(W.chain7_configs(4096), device=dev)
     ms_plain = timed(lambda: cst.is_valid_batch(Q), 5)
+    shape0, _ = autotune.autotune(cst, Q, distances=True)
+    cst.set_fast_launch(*shape0)
     ms_fast = timed(lambda: cst.is_valid_fast(Q, distances=True), 10)
     same = bool(torch.equal(cst.is_valid_fast(Q), cst.is_valid_batch(Q)))
     s1, s2 = W.chain7_edges(1024)
     S1, S2 = torch.tensor(s1, device=dev), torch.tensor(s2, device=dev)
     mv = BoxMotionValidator(cst, [0.05] * 7)
     ms_e_plain = timed(lambda: mv.check_motion_batch(S1, S2), 5)
-    ms_e_fast = timed(lambda: mv.check_motion_fast(S1, S2), 10)
+    eout = torch.empty(S1.shape[0], dtype=torch.uint8, device=dev)
+    ms_e_fast = timed(lambda: mv.check_motion_fast(S1, S2, out=eout), 10)
     same_e = bool(torch.equal(mv.check_motion_fast(S1, S2), mv.check_motion_batch(S1, S2)))
+    try:  # the whole edge pipeline (setup, scan, persistent kernel, recheck) as one CUDA graph
+        eg = _capture(lambda: mv.check_motion_fast(S1, S2, out=eout))
+        ms_e_graph = timed(eg.replay, 10)
+    except Exception:  # noqa: BLE001 - reported as null
+        ms_e_graph = None
     return {
         "C0": {"workload": "7-joint chain, 56 spheres, 10 boxes + 5 spheres + 5 cylinders, 4096 configurations",
                "unit": "configs/s", "plain_fp64": 4096 / (ms_plain / 1e3), "fast_with_distances": 4096 / (ms_fast / 1e3),
-               "ms": {"plain_fp64": ms_plain, "fast_with_distances": ms_fast}, "validity_identical": same},
+               "ms": {"plain_fp64": ms_plain, "fast_with_distances": ms_fast}, "validity_identical": same,
+               "launch_shape": list(shape0)},
         "C1": {"workload": "1024 straight edges on the C0 chain and scene, box validator width 0.05 rad, 1-120 waypoints",
                "unit": "edges/s", "plain_fp64": 1024 / (ms_e_plain / 1e3), "fast_persistent": 1024 / (ms_e_fast / 1e3),
-               "ms": {"plain_fp64": ms_e_plain, "fast_persistent": ms_e_fast}, "edge_validity_identical": same_e},
+               "fast_cuda_graph": 1024 / (ms_e_graph / 1e3) if ms_e_graph else None,
+               "ms": {"plain_fp64": ms_e_plain, "fast_persistent": ms_e_fast, "fast_cuda_graph": ms_e_graph},
+               "edge_validity_identical": same_e},
     }
 
 
@@ -495,9 +508,10 @@ def main():
     alg_bytes = B * (cst.q_dim() * 8 + 1 + ns * 4)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     prof = ROOT / "profiles" / "k_fast_valid_dualarm65536.traffic.json"
-    traffic = None
+    traffic, issue = None, None
     if prof.exists():
-        traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+        pj = json.loads(prof.read_text())
+        traffic, issue = pj.get("dram_bytes_per_launch"), pj.get("issue_active_pct")
 
     side = None
     if rank == 0 and not args.headline_only:
@@ -528,7 +542,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": hbm_kind,
                      "kernel": "k_fast_valid", "kernel_ms": kernel_ms, "launches": k_n,
-                     "note": "HBM is not the binding resource: the kernel is issue/latency bound (see profiles/)"},
+                     "note": "HBM is not the binding resource: the kernel is issue/latency bound"
+                             + (f" (ncu: SM issue active {issue} %, profiles/k_fast_valid_dualarm65536.md)" if issue else "")},
         "clocks": clk.summary(),
         "plain_fp64": {"value": B / (ms_plain / 1e3), "unit": "configs/s", "ms_per_batch": ms_plain,
                        "what": "plain FP64 method, one thread per configuration, validity only"},

@@ -23,6 +23,15 @@ class _ValidatorBase:
         self.cst = cst
         self._width = np.zeros(cst.q_dim())
         self._res = 0.0
+        self._dev_width = {}  # device -> width tensor, made once so device calls copy nothing from the host
+
+    def _width_arg(self, b: Batch) -> Batch:
+        if b.mem == 0:
+            return Batch(self._width)
+        dev = b.keep.device
+        if dev not in self._dev_width:
+            self._dev_width[dev] = _to_device_like(self._width, b)
+        return Batch(self._dev_width[dev])
 
     def _edges(self, S1, S2):
         b1, b2 = Batch(S1), Batch(S2)
@@ -38,21 +47,27 @@ class _ValidatorBase:
         b1, b2 = self._edges(S1, S2)
         E = b1.shape[0]
         out, optr = b1.empty((E,), np.uint8)
-        w = Batch(self._width) if b1.mem == 0 else Batch(_to_device_like(self._width, b1))
+        w = self._width_arg(b1)
         cnt = C.c_int64(0)
         check(lib.pmgpu_check_motion(self.cst._h, b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res), optr, C.byref(cnt), b1.mem,
                                      b1.stream))
         return (out, int(cnt.value)) if return_count else out
 
-    def check_motion_fast(self, S1, S2, stats: bool = False):
-        """FP32 + FP64-recheck persistent work-queue path: (E,) uint8 identical to the plain method."""
+    def check_motion_fast(self, S1, S2, stats: bool = False, out=None):
+        """FP32 + FP64-recheck persistent work-queue path: (E,) uint8 identical to the plain method.
+        With CUDA tensors and stats=False the call only enqueues work on torch's current stream
+        (no host synchronisation, no host copies), so it can be captured in a CUDA graph after one
+        warm-up call; `out` may be a preallocated (E,) uint8 buffer in the same memory space."""
         b1, b2 = self._edges(S1, S2)
         E = b1.shape[0]
-        out, optr = b1.empty((E,), np.uint8)
-        w = Batch(self._width) if b1.mem == 0 else Batch(_to_device_like(self._width, b1))
+        if out is not None:
+            optr = Batch(out, np.uint8).ptr
+        else:
+            out, optr = b1.empty((E,), np.uint8)
+        w = self._width_arg(b1)
         st = np.zeros(4, dtype=np.int64)
         check(lib.pmgpu_check_motion_fast(self.cst._h, b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res), optr,
-                                          C.c_void_p(st.ctypes.data), b1.mem, b1.stream))
+                                          C.c_void_p(st.ctypes.data) if stats else None, b1.mem, b1.stream))
         if stats:
             return out, {"waypoints": int(st[0]), "rechecked_terms": int(st[1]), "edges": int(st[2])}
         return out

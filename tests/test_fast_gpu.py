@@ -174,6 +174,35 @@ def test_fast_edges_match_oracle(chain):
     assert np.array_equal(got, ref)
 
 
+def test_fast_edges_cuda_graph(chain):
+    """All edges in one captured launch sequence: the replayed graph gives the eager booleans,
+    for new edge data copied into the captured input buffers too."""
+    import torch
+
+    (_, cst, _), _ = chain
+    mv = BoxMotionValidator(cst, np.full(7, 0.05))
+    s1, s2 = W.chain7_edges(1024, seed=3)
+    S1, S2 = torch.tensor(s1, device="cuda"), torch.tensor(s2, device="cuda")
+    out = torch.empty(1024, dtype=torch.uint8, device="cuda")
+    mv.check_motion_fast(S1, S2, out=out)  # warm-up: workspaces and tables
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        mv.check_motion_fast(S1, S2, out=out)
+    torch.cuda.current_stream().wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        mv.check_motion_fast(S1, S2, out=out)
+    for seed in (3, 4):
+        a, b = W.chain7_edges(1024, seed=seed)
+        S1.copy_(torch.tensor(a))
+        S2.copy_(torch.tensor(b))
+        out.fill_(7)
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), mv.check_motion_batch(a, b))
+
+
 def test_fast_edges_degenerate(chain):
     (_, cst, _), (_, oc, _) = chain
     q = W.chain7_configs(4, seed=40)
