@@ -72,6 +72,43 @@ class _ValidatorBase:
             return out, {"waypoints": int(st[0]), "rechecked_terms": int(st[1]), "edges": int(st[2])}
         return out
 
+    def shortcut(self, points, fast: bool = True):
+        """Shortcut a path with all candidate edges checked in one batch.
+
+        The reference shortcuts through OMPL's randomised PathSimplifier::partialShortcutPath
+        (ompl/ompl_thin_wrap.hpp:130-170), one checkMotion per candidate.  Here every pair (i, j),
+        j > i + 1, of the path's waypoints is a candidate edge; all are checked at once
+        (check_motion_fast, or the plain method), and the returned path is the shortest (sum of
+        Euclidean segment lengths) through valid candidates and the original segments, found by
+        a forward pass over the waypoints.  Deterministic; the endpoints are kept.  points: (n, q_dim)."""
+        P = f64(points)
+        n = P.shape[0]
+        if P.ndim != 2 or P.shape[1] != self.cst.q_dim():
+            raise ValueError(f"points must be (n, {self.cst.q_dim()})")
+        if n <= 2:
+            return P.copy()
+        ii, jj = np.triu_indices(n, k=2)
+        ok = self.check_motion_fast(P[ii], P[jj]) if fast else self.check_motion_batch(P[ii], P[jj])
+        ok = np.asarray(ok.cpu() if hasattr(ok, "cpu") else ok).astype(bool)
+        best = np.full(n, np.inf)
+        prev = np.full(n, -1)
+        best[0] = 0.0
+        seg = np.linalg.norm(P[1:] - P[:-1], axis=1)
+        by_end = {}
+        for a, b, v in zip(ii, jj, ok):
+            if v:
+                by_end.setdefault(int(b), []).append(int(a))
+        for j in range(1, n):
+            best[j], prev[j] = best[j - 1] + seg[j - 1], j - 1
+            for i in by_end.get(j, []):
+                c = best[i] + float(np.linalg.norm(P[j] - P[i]))
+                if c < best[j]:
+                    best[j], prev[j] = c, i
+        idx = [n - 1]
+        while idx[-1] != 0:
+            idx.append(int(prev[idx[-1]]))
+        return P[idx[::-1]].copy()
+
     def checkMotion(self, s1, s2) -> bool:  # noqa: N802 (OMPL's name)
         d = self.cst.q_dim()
         return bool(self.check_motion_batch(f64(s1, (1, d)), f64(s2, (1, d)))[0])

@@ -203,6 +203,26 @@ def test_fast_edges_cuda_graph(chain):
         assert np.array_equal(out.cpu().numpy(), mv.check_motion_batch(a, b))
 
 
+def test_batched_shortcut(chain):
+    """shortcut(): every returned segment is an original segment or a valid edge of the plain
+    validator, endpoints are kept and the path gets no longer."""
+    (_, cst, _), _ = chain
+    mv = BoxMotionValidator(cst, np.full(7, 0.05))
+    rng = np.random.default_rng(8)
+    # a wandering path through mostly free space: random small steps from a valid start
+    start = W.chain7_configs(256, seed=9)[cst.is_valid_batch(W.chain7_configs(256, seed=9)).astype(bool)][0]
+    path = start + np.cumsum(rng.normal(0, 0.05, (40, 7)), axis=0)
+    out = mv.shortcut(path)
+    assert np.array_equal(out[0], path[0]) and np.array_equal(out[-1], path[-1])
+    length = lambda p: np.linalg.norm(p[1:] - p[:-1], axis=1).sum()  # noqa: E731
+    assert length(out) <= length(path) + 1e-12 and len(out) < len(path)
+    orig = {(tuple(a), tuple(b)) for a, b in zip(path[:-1], path[1:])}
+    new = [(a, b) for a, b in zip(out[:-1], out[1:]) if (tuple(a), tuple(b)) not in orig]
+    if new:
+        assert mv.check_motion_batch(np.array([a for a, _ in new]), np.array([b for _, b in new])).all()
+    assert np.array_equal(mv.shortcut(path, fast=False), out)
+
+
 def test_fast_edges_degenerate(chain):
     (_, cst, _), (_, oc, _) = chain
     q = W.chain7_configs(4, seed=40)

@@ -225,3 +225,27 @@ def test_pose_constraint_construction():
     other = KinematicModel(robot.urdf)
     with pytest.raises(RuntimeError, match="same kinematic chain"):
         IneqCompositeCst([sc, LinkPositionBoundCst(other, j, BaseType.FIXED, robot.end_link, 2, lb=0.1)])
+
+
+def test_sequential_cst_bookkeeping():
+    """SequentialCst dimensions (sequential_constraint.cpp:14-61): add_at range check, fixed points
+    clear their step's constraints at finalize, the motion-step box adds 2 q_dim rows per step."""
+    from plainmp_gb300 import BaseType, KinematicModel, LinkPoseCst
+    from plainmp_gb300.sequential import SequentialCst
+    from plainmp_gb300 import workloads as W
+
+    robot = W.chain7_robot()
+    kin = KinematicModel(robot.urdf)
+    c = LinkPoseCst(kin, robot.control_joints, BaseType.FIXED, [robot.end_link], [np.zeros(3)])
+    s = SequentialCst(5, 7)
+    s.add_globally(c)
+    assert s.cst_dim() == 15 and s.x_dim() == 35
+    with pytest.raises(RuntimeError, match="out of range"):
+        s.add_at(c, 5)
+    s.add_fixed_point_at(np.zeros(7), 0)
+    s.add_fixed_point_at(np.zeros(7), 4)
+    s.add_motion_step_box_constraint(np.full(7, 0.1))
+    assert s.cst_dim() == 15 + 14 + 56
+    s.finalize()
+    assert s.cst_dim() == 9 + 14 + 56
+    assert "fixed point: 7" in str(s)
