@@ -747,20 +747,27 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   }
   __syncthreads();
   const int hq_cap = T->n_clouds > 0 ? CPB * ns : 0;
-  const int n_sph_tasks = ncfg * ns;
-  const int n_tasks = n_sph_tasks + ncfg * npr;
+  // tasks are numbered with the configuration fastest (CPB is a power of two: no division), so
+  // neighbouring threads read the same sphere or pair records
+  const int n_sph_tasks = ns * CPB;
+  const int n_tasks = n_sph_tasks + npr * CPB;
+  const unsigned all_culled = np >= 32 ? 0xffffffffu : ((1u << np) - 1u);
   for (int t = tid; t < n_tasks; t += blockDim.x) {
     if (t < n_sph_tasks) {
-      const int c = t / ns, si = t - c * ns;
-      if (sm.flags[c] & 2) continue;
+      const int si = t / CPB, c = t % CPB;
+      if (c >= ncfg || (sm.flags[c] & 2)) continue;
       const SphereF S = sm.sph[si];
       const GroupF& G = sm.grp[S.group];
       const bool check = !G.only_self && np > 0;
       if (!want_dist && (!check || (sm.flags[c] & FLAG_FAIL))) continue;
+      const unsigned cm = sm.cull[c * ng + S.group];
+      if (np <= 32 && cm == all_culled) {  // the group sphere clears every primitive (by the cutoff too)
+        if (want_dist) sm.sdist[c * ns + si] = f2o(cutoff);
+        continue;
+      }
       const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
       const float3 sc = xf(P, S.x, S.y, S.z);
       const float ek = P[12] + P[13] * S.sn;  // FK error bound of the sphere centre
-      const unsigned cm = sm.cull[c * ng + S.group];
       float sdmin = cutoff;
       int fail = 0;
       const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
@@ -805,8 +812,8 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       if (want_dist) sm.sdist[c * ns + si] = f2o(sdmin);
     } else {
       const int u = t - n_sph_tasks;
-      const int c = u / npr, pi = u - c * npr;
-      if (sm.flags[c] & (FLAG_FAIL | 2)) continue;
+      const int pi = u / CPB, c = u % CPB;
+      if (c >= ncfg || (sm.flags[c] & (FLAG_FAIL | 2))) continue;
       const int2 pr = sm.pairs[pi];
       const GroupF& G1 = sm.grp[pr.x];
       const GroupF& G2 = sm.grp[pr.y];
@@ -893,7 +900,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   }
   __syncthreads();
   if (want_dist)
-    for (int t = tid; t < ncfg * ns; t += blockDim.x) dist32[(c0 + t / ns) * ns + t % ns] = o2f(sm.sdist[t]);
+    for (int t = tid; t < ncfg * ns; t += blockDim.x) dist32[c0 * ns + t] = o2f(sm.sdist[t]);  // sdist is [cfg][sphere]
   __syncthreads();
   if (tid < ncfg && !(sm.flags[tid] & 2)) src.done(c0 + tid, (sm.flags[tid] & FLAG_FAIL) != 0);
   __syncthreads();
@@ -1089,9 +1096,9 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
       const PmPrim& P = v.P[it.y >> 1];
       const PmGroup& g = v.G[v.sgroup[it.z]];
       double cv[3] = {0, 0, 0}, gv[3] = {0, 0, 0};
-      if (lane == 0) {
+      if (lane == 0) {  // only the slot's chain of ancestors
         DPose pose[PM_MAX_SLOTS];
-        fk64(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, pose);
+        fk64_need(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, g.slot), pose);
         const DM3 R = qmat(pose[g.slot].q);
         const D3 gc = add(mv(R, D3{g.rel[0], g.rel[1], g.rel[2]}), pose[g.slot].t);
         const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
@@ -1123,11 +1130,11 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
         hit = !outside_aabb(P, c, r) && !prim_outside(P, v.C, c, r);
       }
     } else if (lane == 0) {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test
-      DPose pose[PM_MAX_SLOTS];
-      fk64(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, pose);
       const int pr = it.y >> 1;
       const PmGroup& g1 = v.G[v.pairs[2 * pr]];
       const PmGroup& g2 = v.G[v.pairs[2 * pr + 1]];
+      DPose pose[PM_MAX_SLOTS];
+      fk64_need(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, g1.slot) | slot_chain(T, g2.slot), pose);
       const DM3 R1 = qmat(pose[g1.slot].q), R2 = qmat(pose[g2.slot].q);
       const D3 c1 = add(mv(R1, D3{g1.rel[0], g1.rel[1], g1.rel[2]}), pose[g1.slot].t);
       const D3 c2 = add(mv(R2, D3{g2.rel[0], g2.rel[1], g2.rel[2]}), pose[g2.slot].t);

@@ -215,6 +215,39 @@ __device__ __forceinline__ void fk64(const PmTablesHdr* T, const double* state, 
   }
 }
 
+// The same FK restricted to the slots whose bit is set in `need` (a set closed under parents,
+// e.g. from slot_chain); the values of those slots are the full FK's, bit for bit.
+__device__ __forceinline__ uint64_t slot_chain(const PmTablesHdr* T, int slot) {
+  const PmSlot* S = pm_at<PmSlot>(T, T->off_slots);
+  uint64_t m = 0;
+  for (int i = slot; i >= 0; i = S[i].parent) m |= 1ull << i;
+  return m;
+}
+template <class PoseArr>
+__device__ __forceinline__ void fk64_need(const PmTablesHdr* T, const double* state, const double* q, bool taylor, uint64_t need,
+                                          PoseArr& pose) {
+  const PmSlot* S = pm_at<PmSlot>(T, T->off_slots);
+  for (int i = 0; i < T->n_slots; i++) {
+    if (!((need >> i) & 1ull)) continue;
+    const PmSlot& s = S[i];
+    if (s.parent < 0) {
+      pose[i] = base_pose(T, state, q, T->n_ctrl);
+      continue;
+    }
+    DQ lq;
+    D3 lt;
+    bool lid;
+    if (s.mode == PM_FK_STATE) {
+      DPose l = state_pose(state, PM_STATE_LINK_ROW(s.link), lid);
+      lq = l.q;
+      lt = l.t;
+    } else {
+      joint_local(s, q[s.qcol], taylor, lq, lt, lid);
+    }
+    pose[i] = compose(pose[s.parent], lq, lt, lid);
+  }
+}
+
 // ------------------------------------------------------------------------- transforms for jacobians
 __device__ __forceinline__ DPose pose_inverse(const DPose& a) {  // transform.hpp:88-91
   double n2 = (a.q.x * a.q.x + a.q.y * a.q.y) + (a.q.z * a.q.z + a.q.w * a.q.w);
