@@ -1,0 +1,46 @@
+"""Small, self-contained launches of the differentiable-cost kernels for profiling: one fused IK
+descent (8192 problems x 50 steps, the C3 workload) and one trajectory cost + gradient (512
+trajectories, the C4 workload).  python -m plainmp_gb300.profile_cases [ik|traj|all]"""
+import sys
+
+import numpy as np
+
+
+def ik(steps: int = 50):
+    import torch
+
+    from plainmp_gb300 import diff, scenes
+    from plainmp_gb300 import workloads as W
+
+    robot, scene = W.chain7_robot(), W.chain7_scene()
+    kin, cst, _ = scenes.make_constraint(robot, scene)
+    link = kin.get_link_ids([robot.end_link])[0]
+    q0, q_star = W.ik_problems(8192)
+    tgt = diff.link_poses(cst, torch.tensor(q_star, device="cuda"), link).float()
+    Q0 = torch.tensor(q0, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        diff.ik_descend(cst, Q0, tgt, link, steps=steps, lr=0.05)
+    torch.cuda.synchronize()
+
+
+def traj():
+    import torch
+
+    from plainmp_gb300 import diff, scenes
+    from plainmp_gb300 import workloads as W
+
+    _, cst, _ = scenes.make_constraint(W.planar_chain7_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0))
+    trajs = W.trajectories(512)
+    Q = torch.tensor(np.concatenate(trajs, axis=0).astype(np.float32), device="cuda")
+    off = torch.tensor(np.concatenate([[0], np.cumsum([len(t) for t in trajs])]).astype(np.int64), device="cuda")
+    for _ in range(2):
+        diff.traj_cost_grad(cst, Q, off)
+    torch.cuda.synchronize()
+
+
+if __name__ == "__main__":
+    which = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if which in ("ik", "all"):
+        ik()
+    if which in ("traj", "all"):
+        traj()
