@@ -406,7 +406,14 @@ def main():
     import plainmp_gb300 as pm
     from plainmp_gb300 import _lib, scenes
 
-    robot, scene, qh = workload()
+    from plainmp_gb300 import replicas
+
+    robot, scene, _ = workload()
+    # weak scaling: every rank checks its own B-configuration slice of a world * B batch
+    from plainmp_gb300 import workloads as W
+
+    a, b = replicas.shard(world * B, rank, world)
+    qh = W.dualarm_configs(world * B)[a:b] if world > 1 else W.dualarm_configs(B)
     kin, cst, sdf = scenes.make_constraint(robot, scene)
     dev = torch.device("cuda", local)
     Q = torch.tensor(qh, device=dev)
@@ -453,10 +460,7 @@ def main():
     r_ms, r_n = _lib.profile_read("k_fast_recheck")
     rest_ms, rest_n = _lib.profile_read("*")
     all_n = k_n + r_n + rest_n
-    t = torch.tensor([total_ms], device=dev)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(total_ms, dist, dev)
     ms_per_step = total_ms / args.steps
     value = world * B * args.steps / (total_ms / 1e3)
 
