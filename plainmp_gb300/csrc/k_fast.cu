@@ -1095,25 +1095,12 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
     if ((it.y & 1) == 0) {  // sphere it.z vs primitive it.y >> 1: gate AND test
       const PmPrim& P = v.P[it.y >> 1];
       const PmGroup& g = v.G[v.sgroup[it.z]];
-      double cv[3] = {0, 0, 0}, gv[3] = {0, 0, 0};
-      if (lane == 0) {  // only the slot's chain of ancestors
-        DPose pose[PM_MAX_SLOTS];
-        fk64_need(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, g.slot), pose);
-        const DM3 R = qmat(pose[g.slot].q);
-        const D3 gc = add(mv(R, D3{g.rel[0], g.rel[1], g.rel[2]}), pose[g.slot].t);
-        const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
-        cv[0] = c.x;
-        cv[1] = c.y;
-        cv[2] = c.z;
-        gv[0] = gc.x;
-        gv[1] = gc.y;
-        gv[2] = gc.z;
-      }
-      for (int k = 0; k < 3; k++) {
-        cv[k] = __shfl_sync(FULL, cv[k], 0);
-        gv[k] = __shfl_sync(FULL, gv[k], 0);
-      }
-      const D3 c{cv[0], cv[1], cv[2]}, gc{gv[0], gv[1], gv[2]};
+      // the FP64 FK of the slot's chain of ancestors, by the whole warp (every lane gets the poses)
+      DPose pose[PM_MAX_SLOTS];
+      fk64_need_warp(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, g.slot), pose);
+      const DM3 R = qmat(pose[g.slot].q);
+      const D3 gc = add(mv(R, D3{g.rel[0], g.rel[1], g.rel[2]}), pose[g.slot].t);
+      const D3 c = add(mv(R, v.rel(it.z)), pose[g.slot].t);
       const double r = v.sr[it.z];
       if (P.kind == PM_SDF_CLOUD) {
         // the sphere's own test first (small reach); its nearest point then settles the gate
@@ -1129,12 +1116,13 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
       } else if (lane == 0 && !outside_aabb(P, gc, g.radius) && !prim_outside(P, v.C, gc, g.radius)) {
         hit = !outside_aabb(P, c, r) && !prim_outside(P, v.C, c, r);
       }
-    } else if (lane == 0) {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test
+    } else {  // sphere pair (it.z, it.w) of self pair it.y >> 1: gate AND test (every lane, same values)
       const int pr = it.y >> 1;
       const PmGroup& g1 = v.G[v.pairs[2 * pr]];
       const PmGroup& g2 = v.G[v.pairs[2 * pr + 1]];
       DPose pose[PM_MAX_SLOTS];
-      fk64_need(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, g1.slot) | slot_chain(T, g2.slot), pose);
+      fk64_need_warp(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, g1.slot) | slot_chain(T, g2.slot),
+                     pose);
       const DM3 R1 = qmat(pose[g1.slot].q), R2 = qmat(pose[g2.slot].q);
       const D3 c1 = add(mv(R1, D3{g1.rel[0], g1.rel[1], g1.rel[2]}), pose[g1.slot].t);
       const D3 c2 = add(mv(R2, D3{g2.rel[0], g2.rel[1], g2.rel[2]}), pose[g2.slot].t);

@@ -248,6 +248,87 @@ __device__ __forceinline__ void fk64_need(const PmTablesHdr* T, const double* st
   }
 }
 
+// Warp-cooperative fk64_need for latency-bound single configurations (all 32 lanes, identical
+// arguments; every lane ends with the poses).  Each lane computes the local transform of one slot;
+// then, slot by slot, lanes 0-3 compute the four components of the quaternion product and lanes
+// 0-2 the three components of the rotated translation.  Every component is evaluated with the
+// expression (operand pairs, signs, summation order) of qmul / qrot / add, so the poses are bit for
+// bit those of fk64_need; lanes differ only in which operands they select, so the warp does not
+// diverge.  GB300 issues an FP64 warp instruction at a cost that does not shrink with inactive
+// lanes, so spreading the components cuts the dependent FP64 chain per slot from 61 to 18.
+__device__ __forceinline__ double sel4(int k, double a0, double a1, double a2, double a3) {
+  return k == 0 ? a0 : (k == 1 ? a1 : (k == 2 ? a2 : a3));
+}
+__device__ __forceinline__ double neg_if(bool n, double v) {
+  return __longlong_as_double(__double_as_longlong(v) ^ (n ? (long long)0x8000000000000000ull : 0ll));
+}
+template <class PoseArr>
+__device__ void fk64_need_warp(const PmTablesHdr* T, const double* state, const double* q, bool taylor, uint64_t need, PoseArr& pose) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const PmSlot* S = pm_at<PmSlot>(T, T->off_slots);
+  const int n = T->n_slots;
+  // component index of this lane (lanes 4-31 repeat lanes 0-3; their results are not used)
+  const int k4 = lane & 3, k3 = lane % 3;
+  for (int base = 0; base < n; base += 32) {
+    const int i = base + lane;
+    DQ lq{0, 0, 0, 1};
+    D3 lt{0, 0, 0};
+    bool lid = true;
+    if (i < n && ((need >> i) & 1ull) && S[i].parent >= 0) {
+      const PmSlot& s = S[i];
+      if (s.mode == PM_FK_STATE) {
+        const DPose l = state_pose(state, PM_STATE_LINK_ROW(s.link), lid);
+        lq = l.q;
+        lt = l.t;
+      } else {
+        joint_local(s, q[s.qcol], taylor, lq, lt, lid);
+      }
+    }
+    for (int k = 0; k < 32 && base + k < n; k++) {
+      const int si = base + k;
+      if (!((need >> si) & 1ull)) continue;
+      const PmSlot& s = S[si];
+      if (s.parent < 0) {
+        pose[si] = base_pose(T, state, q, T->n_ctrl);
+        continue;
+      }
+      const DQ b{__shfl_sync(FULL, lq.x, k), __shfl_sync(FULL, lq.y, k), __shfl_sync(FULL, lq.z, k), __shfl_sync(FULL, lq.w, k)};
+      const D3 v{__shfl_sync(FULL, lt.x, k), __shfl_sync(FULL, lt.y, k), __shfl_sync(FULL, lt.z, k)};
+      const bool id = __shfl_sync(FULL, lid ? 1 : 0, k) != 0;
+      const DPose P = pose[s.parent];
+      const DQ& a = P.q;
+      DPose o;
+      if (id) {
+        o.q = a;
+      } else {
+        // qmul(a, b): w: aw*bw - ax*bx - ay*by - az*bz;  x: aw*bx + ax*bw + ay*bz - az*by;
+        //             y: aw*by + ay*bw + az*bx - ax*bz;   z: aw*bz + az*bw + ax*by - ay*bx
+        const double p0 = a.w * sel4(k4, b.w, b.x, b.y, b.z);
+        const double p1 = sel4(k4, a.x, a.x, a.y, a.z) * sel4(k4, b.x, b.w, b.w, b.w);
+        const double p2 = sel4(k4, a.y, a.y, a.z, a.x) * sel4(k4, b.y, b.z, b.x, b.y);
+        const double p3 = sel4(k4, a.z, a.z, a.x, a.y) * sel4(k4, b.z, b.y, b.z, b.x);
+        const double r = ((p0 + neg_if(k4 == 0, p1)) + neg_if(k4 == 0, p2)) - p3;
+        o.q = DQ{__shfl_sync(FULL, r, 1), __shfl_sync(FULL, r, 2), __shfl_sync(FULL, r, 3), __shfl_sync(FULL, r, 0)};
+      }
+      // qrot(a, v): uv = cross(a.vec, v); uv += uv; c = cross(a.vec, uv); (v + a.w * uv) + c; then add(P.t, .)
+      const D3 av{a.x, a.y, a.z};
+      const double u1 = sel4(k3, av.y, av.z, av.x, 0.0) * sel4(k3, v.z, v.x, v.y, 0.0);
+      const double u2 = sel4(k3, av.z, av.x, av.y, 0.0) * sel4(k3, v.y, v.z, v.x, 0.0);
+      double uvk = u1 - u2;
+      uvk = uvk + uvk;
+      const D3 uv{__shfl_sync(FULL, uvk, 0), __shfl_sync(FULL, uvk, 1), __shfl_sync(FULL, uvk, 2)};
+      const double c1 = sel4(k3, av.y, av.z, av.x, 0.0) * sel4(k3, uv.z, uv.x, uv.y, 0.0);
+      const double c2 = sel4(k3, av.z, av.x, av.y, 0.0) * sel4(k3, uv.y, uv.z, uv.x, 0.0);
+      const double ck = c1 - c2;
+      const double rk = (sel4(k3, v.x, v.y, v.z, 0.0) + a.w * sel4(k3, uv.x, uv.y, uv.z, 0.0)) + ck;
+      const double tk = sel4(k3, P.t.x, P.t.y, P.t.z, 0.0) + rk;
+      o.t = D3{__shfl_sync(FULL, tk, 0), __shfl_sync(FULL, tk, 1), __shfl_sync(FULL, tk, 2)};
+      pose[si] = o;
+    }
+  }
+}
+
 // ------------------------------------------------------------------------- transforms for jacobians
 __device__ __forceinline__ DPose pose_inverse(const DPose& a) {  // transform.hpp:88-91
   double n2 = (a.q.x * a.q.x + a.q.y * a.q.y) + (a.q.z * a.q.z + a.q.w * a.q.w);
