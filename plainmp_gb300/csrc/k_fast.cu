@@ -752,97 +752,123 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   const int n_sph_tasks = ns * CPB;
   const int n_tasks = n_sph_tasks + npr * CPB;
   const unsigned all_culled = np >= 32 ? 0xffffffffu : ((1u << np) - 1u);
-  for (int t = tid; t < n_tasks; t += blockDim.x) {
+  // one sphere of one configuration: primitives in-thread, cloud queries near the cloud queued
+  auto sphere_task = [&](int si, int c) {
+    if (c >= ncfg || (sm.flags[c] & 2)) return;
+    const SphereF S = sm.sph[si];
+    const GroupF& G = sm.grp[S.group];
+    const bool check = !G.only_self && np > 0;
+    if (!want_dist && (!check || (sm.flags[c] & FLAG_FAIL))) return;
+    const unsigned cm = sm.cull[c * ng + S.group];
+    if (np <= 32 && cm == all_culled) {  // the group sphere clears every primitive (by the cutoff too)
+      if (want_dist) sm.sdist[c * ns + si] = f2o(cutoff);
+      return;
+    }
+    const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
+    const float3 sc = xf(P, S.x, S.y, S.z);
+    const float ek = P[12] + P[13] * S.sn;  // FK error bound of the sphere centre
+    float sdmin = cutoff;
+    int fail = 0;
+    const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
+    for (int p = 0; p < np; p++) {
+      if (p < 32 && ((cm >> p) & 1u)) continue;
+      const PrimF& Pr = sm.prm[p];
+      float g, sd, mag;
+      if (Pr.kind == PM_SDF_CLOUD) {
+        const PmGridDev& Gc = v.C[Pr.cloud];
+        const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z);
+        const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
+        if (fb.lb - Pr.a - S.r > margin32(qmag + fb.lb) + ek + (want_dist ? cutoff : 0.f)) continue;
+        if (!want_dist && check && fb.idx >= 0) {
+          // the centre's nearest point is a real point: if it is certainly within reach, the
+          // sphere collides and no search is needed
+          const float ub = sqrtf(point_d2_32(Gc, fb.idx, sc.x, sc.y, sc.z));
+          if (ub - Pr.a - S.r < -(margin32(qmag + ub) + ek)) {
+            fail = 1;
+            break;
+          }
+        }
+        const int k = atomicAdd(&sm.hq_n[0], 1);
+        if (k < hq_cap) {
+          sm.hq[k] = make_int2(c * ns + si, p);
+          continue;
+        }
+        clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, want_dist ? m + cutoff : m, g, sd, mag);
+      } else {
+        clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, 0.f, g, sd, mag);
+      }
+      sdmin = fminf(sdmin, sd);
+      if (!check) continue;
+      const float mm = margin32(mag) + ek;
+      if (g < -mm) {
+        fail = 1;
+        if (!want_dist) break;
+      } else if (g <= mm) {
+        push_item(scr, src, (int)(c0 + c), p << 1, si, 0);
+      }
+    }
+    if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
+    if (want_dist) sm.sdist[c * ns + si] = f2o(sdmin);
+  };
+  // Self pairs: each lane tests its (configuration, group pair) by the group spheres; the warp then
+  // takes the surviving pairs one at a time, 32 sphere pairs per step (rows of 8 x 4), so a rare
+  // survivor does not hold 31 idle lanes for its whole sphere-pair loop.
+  const unsigned FULL = 0xffffffffu;
+  const int lane = tid & 31;
+  for (int t0 = tid & ~31; t0 < n_tasks; t0 += blockDim.x) {  // warp-uniform
+    const int t = t0 + lane;
+    int hit_pi = -1, hit_c = 0;
     if (t < n_sph_tasks) {
-      const int si = t / CPB, c = t % CPB;
-      if (c >= ncfg || (sm.flags[c] & 2)) continue;
-      const SphereF S = sm.sph[si];
-      const GroupF& G = sm.grp[S.group];
-      const bool check = !G.only_self && np > 0;
-      if (!want_dist && (!check || (sm.flags[c] & FLAG_FAIL))) continue;
-      const unsigned cm = sm.cull[c * ng + S.group];
-      if (np <= 32 && cm == all_culled) {  // the group sphere clears every primitive (by the cutoff too)
-        if (want_dist) sm.sdist[c * ns + si] = f2o(cutoff);
-        continue;
-      }
-      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
-      const float3 sc = xf(P, S.x, S.y, S.z);
-      const float ek = P[12] + P[13] * S.sn;  // FK error bound of the sphere centre
-      float sdmin = cutoff;
-      int fail = 0;
-      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
-      for (int p = 0; p < np; p++) {
-        if (p < 32 && ((cm >> p) & 1u)) continue;
-        const PrimF& Pr = sm.prm[p];
-        float g, sd, mag;
-        if (Pr.kind == PM_SDF_CLOUD) {
-          const PmGridDev& Gc = v.C[Pr.cloud];
-          const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z);
-          const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
-          if (fb.lb - Pr.a - S.r > margin32(qmag + fb.lb) + ek + (want_dist ? cutoff : 0.f)) continue;
-          if (!want_dist && check && fb.idx >= 0) {
-            // the centre's nearest point is a real point: if it is certainly within reach, the
-            // sphere collides and no search is needed
-            const float ub = sqrtf(point_d2_32(Gc, fb.idx, sc.x, sc.y, sc.z));
-            if (ub - Pr.a - S.r < -(margin32(qmag + ub) + ek)) {
-              fail = 1;
-              break;
-            }
-          }
-          const int k = atomicAdd(&sm.hq_n[0], 1);
-          if (k < hq_cap) {
-            sm.hq[k] = make_int2(c * ns + si, p);
-            continue;
-          }
-          clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, want_dist ? m + cutoff : m, g, sd, mag);
-        } else {
-          clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, 0.f, g, sd, mag);
-        }
-        sdmin = fminf(sdmin, sd);
-        if (!check) continue;
-        const float mm = margin32(mag) + ek;
-        if (g < -mm) {
-          fail = 1;
-          if (!want_dist) break;
-        } else if (g <= mm) {
-          push_item(scr, src, (int)(c0 + c), p << 1, si, 0);
-        }
-      }
-      if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
-      if (want_dist) sm.sdist[c * ns + si] = f2o(sdmin);
-    } else {
+      sphere_task(t / CPB, t % CPB);
+    } else if (t < n_tasks) {
       const int u = t - n_sph_tasks;
       const int pi = u / CPB, c = u % CPB;
-      if (c >= ncfg || (sm.flags[c] & (FLAG_FAIL | 2))) continue;
+      if (c < ncfg && !(sm.flags[c] & (FLAG_FAIL | 2))) {
+        const int2 pr = sm.pairs[pi];
+        const GroupF& G1 = sm.grp[pr.x];
+        const GroupF& G2 = sm.grp[pr.y];
+        const float* P1 = sm.pose + ((size_t)c * nsl + G1.slot) * kPoseF;
+        const float* P2 = sm.pose + ((size_t)c * nsl + G2.slot) * kPoseF;
+        const float3 a = xf(P1, G1.rel[0], G1.rel[1], G1.rel[2]);
+        const float3 bb = xf(P2, G2.rel[0], G2.rel[1], G2.rel[2]);
+        const float ddx = a.x - bb.x, ddy = a.y - bb.y, ddz = a.z - bb.z;
+        const float gmag = fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(bb.x) + fabsf(bb.y) + fabsf(bb.z);
+        if (!(sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz))) - (G1.radius + G2.radius) >
+              2.0f * margin32(gmag) + P1[12] + P1[13] * G1.gn + P2[12] + P2[13] * G2.gn)) {
+          hit_pi = pi;
+          hit_c = c;
+        }
+      }
+    }
+    unsigned pend = __ballot_sync(FULL, hit_pi >= 0);
+    while (pend) {
+      const int src_lane = __ffs(pend) - 1;
+      pend &= pend - 1;
+      const int pi = __shfl_sync(FULL, hit_pi, src_lane), c = __shfl_sync(FULL, hit_c, src_lane);
       const int2 pr = sm.pairs[pi];
       const GroupF& G1 = sm.grp[pr.x];
       const GroupF& G2 = sm.grp[pr.y];
       const float* P1 = sm.pose + ((size_t)c * nsl + G1.slot) * kPoseF;
       const float* P2 = sm.pose + ((size_t)c * nsl + G2.slot) * kPoseF;
-      const float3 a = xf(P1, G1.rel[0], G1.rel[1], G1.rel[2]);
-      const float3 bb = xf(P2, G2.rel[0], G2.rel[1], G2.rel[2]);
-      const float ddx = a.x - bb.x, ddy = a.y - bb.y, ddz = a.z - bb.z;
-      const float gmag = fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(bb.x) + fabsf(bb.y) + fabsf(bb.z);
-      if (sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz))) - (G1.radius + G2.radius) >
-          2.0f * margin32(gmag) + P1[12] + P1[13] * G1.gn + P2[12] + P2[13] * G2.gn)
-        continue;
       int fail = 0;
-      for (int i = G1.begin; i < G1.begin + G1.count && !fail; i++) {
-        const SphereF Si = sm.sph[i];
-        const float3 ci = xf(P1, Si.x, Si.y, Si.z);
-        for (int j = G2.begin; j < G2.begin + G2.count; j++) {
-          const SphereF Sj = sm.sph[j];
-          const float3 cj = xf(P2, Sj.x, Sj.y, Sj.z);
-          const float ex = ci.x - cj.x, ey = ci.y - cj.y, ez = ci.z - cj.z;
-          const float g = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))) - (Si.r + Sj.r);
-          const float mm = 2.0f * margin32(fabsf(ci.x) + fabsf(ci.y) + fabsf(ci.z) + fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z)) +
-                           P1[12] + P1[13] * Si.sn + P2[12] + P2[13] * Sj.sn;
-          if (g < -mm) {
-            fail = 1;
-            break;
+      for (int jb = 0; jb < G2.count; jb += 8) {
+        const int j = jb + (lane & 7);
+        for (int ib = 0; ib < G1.count; ib += 4) {
+          const int i = ib + (lane >> 3);
+          if (i < G1.count && j < G2.count) {
+            const SphereF Si = sm.sph[G1.begin + i];
+            const SphereF Sj = sm.sph[G2.begin + j];
+            const float3 ci = xf(P1, Si.x, Si.y, Si.z);
+            const float3 cj = xf(P2, Sj.x, Sj.y, Sj.z);
+            const float ex = ci.x - cj.x, ey = ci.y - cj.y, ez = ci.z - cj.z;
+            const float g = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))) - (Si.r + Sj.r);
+            const float mm = 2.0f * margin32(fabsf(ci.x) + fabsf(ci.y) + fabsf(ci.z) + fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z)) +
+                             P1[12] + P1[13] * Si.sn + P2[12] + P2[13] * Sj.sn;
+            if (g < -mm) fail = 1;
+            else if (g <= mm) push_item(scr, src, (int)(c0 + c), (pi << 1) | 1, G1.begin + i, G2.begin + j);
           }
-          if (g <= mm) push_item(scr, src, (int)(c0 + c), (pi << 1) | 1, i, j);
         }
+        if (__any_sync(FULL, fail)) break;
       }
       if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
     }
