@@ -470,29 +470,55 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
   return r;
 }
 
-// Warp-cooperative exact FP64 nearest neighbour below maxd2 (the value of grid_nearest64: the
-// minimum over points of fl(dx*dx + (dy*dy + dz*dz)), pruned by the same conservative boxes).
-// The cube of blocks around q within sqrt(maxd2), one block of slack per side for the rounding
-// of the block assignment, is split across lanes; a candidate block's occupied cells are split
-// across lanes and the warp minimum is shared after every block.  For the few FP64 rechecks,
-// where a single thread's walk would be a long serial chain of FP64 operations and loads.
-__device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, double maxd2) {
+// Warp-cooperative exact FP64 nearest neighbour below maxd2: the minimum over points of
+// fl(dx*dx + (dy*dy + dz*dz)) in FP64, as grid_nearest64.  The cube of blocks around q within
+// sqrt(maxd2), one block of slack per side, is split across lanes; a candidate block's occupied
+// cells are split across lanes and the warp minimum is shared after every block.
+// The pruning runs in FP32 and only the points it cannot rule out reach FP64 (the FP64 pipe
+// takes a whole warp instruction per operation, however few lanes are active): a block, cell or
+// point is skipped when its FP32 distance from q exceeds the current best by more than the FP32
+// error of both (t = 4e-7 (|q|_1 + |p|_1 max) + 4e-6 d, far above the rounding of the points,
+// of q and of the distance arithmetic), so no point below the best is ever skipped.  hint: a
+// point index whose distance starts the search (e.g. the FP32 nearest point), or -1.
+__device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, double maxd2, int hint = -1) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   NNResult64 r{maxd2, -1};
   if (G.n_points <= 0 || !(maxd2 > 0.0)) return r;
   double best = maxd2;
   int bidx = -1;
-  const double reach = sqrt(maxd2);
-  const double qa[3] = {q.x, q.y, q.z};
+  if (hint >= 0 && hint < G.n_points) {
+    const D3 d{G.px[hint] - q.x, G.py[hint] - q.y, G.pz[hint] - q.z};
+    const double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
+    if (d2 < best) {
+      best = d2;
+      bidx = hint;
+    }
+  }
+  const float qx = (float)q.x, qy = (float)q.y, qz = (float)q.z;
+  float pmax = 0.f;
+  for (int a = 0; a < 3; a++) pmax += fmaxf(fabsf(G.box_lo32[a]), fabsf(G.box_hi32[a]));
+  const float tabs = 4e-7f * (fabsf(qx) + fabsf(qy) + fabsf(qz) + pmax) + 1e-12f;
+  // FP32 threshold on squared distances: anything above it is farther than the best
+  auto thr = [&](double b) {
+    const float sb = sqrtf((float)b) * (1.0f + 4e-6f) + tabs;
+    return sb * sb * (1.0f + 1e-6f);
+  };
+  float t32 = thr(best);
+  const float reach = sqrtf((float)maxd2) * (1.0f + 1e-6f);
+  const float qa[3] = {qx, qy, qz};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
   int lo[3], hi[3];
   for (int a = 0; a < 3; a++) {
-    const double f0 = floor((qa[a] - reach - G.origin[a]) / G.block) - 1.0;
-    const double f1 = floor((qa[a] + reach - G.origin[a]) / G.block) + 1.0;
-    if (!(f1 >= 0.0) || !(f0 <= (double)(nb[a] - 1))) return r;  // also rejects NaN
-    lo[a] = f0 < 0.0 ? 0 : (int)f0;
-    hi[a] = f1 > (double)(nb[a] - 1) ? nb[a] - 1 : (int)f1;
+    const float f0 = floorf((qa[a] - reach - G.o32[a]) * G.inv_blk32) - 1.0f;
+    const float f1 = floorf((qa[a] + reach - G.o32[a]) * G.inv_blk32) + 1.0f;
+    if (!(f1 >= 0.f) || !(f0 <= (float)(nb[a] - 1))) {  // also rejects NaN
+      r.d2 = best;
+      r.idx = bidx;
+      return r;
+    }
+    lo[a] = f0 < 0.f ? 0 : (int)f0;
+    hi[a] = f1 > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f1;
   }
   const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
   const int nblk = nx * ny * nz;
@@ -506,7 +532,7 @@ __device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, dou
       const int by = lo[1] + t % ny, bz = lo[2] + t / ny;
       const int b = bx + nb[0] * (by + nb[1] * bz);
       occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + b);
-      cand = occ.x < occ.y && box_d2_64(G.blk_box + 6 * b, q) < best;
+      cand = occ.x < occ.y && !(box_d2_32(G.blk_box + 6 * b, qx, qy, qz) > t32);
     }
     unsigned bal = __ballot_sync(FULL, cand);
     while (bal) {
@@ -514,25 +540,33 @@ __device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, dou
       bal &= bal - 1;
       const int c0 = __shfl_sync(FULL, occ.x, src), c1 = __shfl_sync(FULL, occ.y, src);
       for (int c = c0 + lane; c < c1; c += 32) {
-        if (box_d2_64(G.cell_box + 6 * c, q) >= best) continue;
+        if (box_d2_32(G.cell_box + 6 * c, qx, qy, qz) > t32) continue;
         const int2 pr = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + c);
         for (int p = pr.x; p < pr.y; p++) {
+          const float4 pt = __ldg(G.p32 + p);
+          const float ex = pt.x - qx, ey = pt.y - qy, ez = pt.z - qz;
+          if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > t32) continue;
           const D3 d{G.px[p] - q.x, G.py[p] - q.y, G.pz[p] - q.z};
           const double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
-          if (d2 < best) {
+          if (d2 < best || (d2 == best && bidx >= 0 && p < bidx)) {
             best = d2;
             bidx = p;
+            t32 = thr(best);
           }
         }
       }
+      // warp minimum; best >= 0, so its bits order like its value
+      long long bb = __double_as_longlong(best);
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(FULL, best, o);
+        const long long ob = __shfl_xor_sync(FULL, bb, o);
         const int oi = __shfl_xor_sync(FULL, bidx, o);
-        if (ob < best || (ob == best && oi >= 0 && (bidx < 0 || oi < bidx))) {
-          best = ob;
+        if (ob < bb || (ob == bb && oi >= 0 && (bidx < 0 || oi < bidx))) {
+          bb = ob;
           bidx = oi;
         }
       }
+      best = __longlong_as_double(bb);
+      t32 = thr(best);
     }
   }
   r.d2 = best;
@@ -542,9 +576,10 @@ __device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, dou
 
 // is_outside(p, r) of a point cloud (primitive_sdf.hpp:597-603) with the warp search: only
 // whether a point lies within r + radius matters (see prim_outside).  Warp-uniform arguments.
-__device__ __forceinline__ bool cloud_outside_warp(const PmPrim& P, const PmGridDev* clouds, const D3& p, double r, int* near) {
+__device__ __forceinline__ bool cloud_outside_warp(const PmPrim& P, const PmGridDev* clouds, const D3& p, double r, int* near,
+                                                   int hint = -1) {
   const double reach = (r + P.a) * (1.0 + 1e-12) + 1e-12;
-  const NNResult64 nn = warp_nearest64(clouds[P.cloud], p, reach * reach);
+  const NNResult64 nn = warp_nearest64(clouds[P.cloud], p, reach * reach, hint);
   if (near) *near = nn.idx;
   if (nn.idx < 0) return true;
   return sqrt(nn.d2) - P.a > r;
@@ -804,7 +839,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         fail = 1;
         if (!want_dist) break;
       } else if (g <= mm) {
-        push_item(scr, src, (int)(c0 + c), p << 1, si, 0);
+        push_item(scr, src, (int)(c0 + c), p << 1, si, -1);
       }
     }
     if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
@@ -918,7 +953,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
           if (g < -mm) {
             atomicOr(&sm.flags[c], FLAG_FAIL);
           } else if (g <= mm) {
-            push_item(scr, src, (int)(c0 + c), e.y << 1, si, 0);
+            push_item(scr, src, (int)(c0 + c), e.y << 1, si, nn.idx);
           }
         }
       }
@@ -1133,7 +1168,7 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
         // exactly unless rounding leaves it undecided: min_p |gc - p| <= |gc - p_near|
         const PmGridDev& Gd = v.C[P.cloud];
         int near = -1;
-        bool test = !outside_aabb(P, c, r) && !cloud_outside_warp(P, v.C, c, r, &near);
+        bool test = !outside_aabb(P, c, r) && !cloud_outside_warp(P, v.C, c, r, &near, it.w);
         if (test && !outside_aabb(P, gc, g.radius)) {
           const D3 d{Gd.px[near] - gc.x, Gd.py[near] - gc.y, Gd.pz[near] - gc.z};
           const double d2n = d.x * d.x + (d.y * d.y + d.z * d.z);

@@ -1,9 +1,25 @@
-"""Small, self-contained launches of the differentiable-cost kernels for profiling: one fused IK
-descent (8192 problems x 50 steps, the C3 workload) and one trajectory cost + gradient (512
-trajectories, the C4 workload).  python -m plainmp_gb300.profile_cases [ik|traj|all]"""
+"""Small, self-contained launches for profiling: the fast collision check of 65,536 dual-arm
+configurations against the 200k-point box-surface cloud, validity only (``valid``) or with the
+per-sphere distances (``dist``), three launches each; one fused IK descent (8192 problems x 50
+steps, ``ik``); one trajectory cost + gradient (512 trajectories, ``traj``).
+python -m plainmp_gb300.profile_cases [valid|dist|ik|traj|all]"""
 import sys
 
 import numpy as np
+
+
+def fast(distances: bool, n: int = 65536, launches: int = 3):
+    import torch
+
+    from plainmp_gb300 import scenes
+    from plainmp_gb300 import workloads as W
+
+    _, cst, _ = scenes.make_constraint(W.dualarm_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0))
+    cst.set_fast_launch(32, 512)
+    Q = torch.tensor(W.dualarm_configs(n), device="cuda")
+    for _ in range(launches):
+        cst.is_valid_fast(Q, distances=distances)
+    torch.cuda.synchronize()
 
 
 def ik(steps: int = 50):
@@ -40,6 +56,10 @@ def traj():
 
 if __name__ == "__main__":
     which = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if which in ("valid", "all"):
+        fast(False)
+    if which in ("dist", "all"):
+        fast(True)
     if which in ("ik", "all"):
         ik()
     if which in ("traj", "all"):
