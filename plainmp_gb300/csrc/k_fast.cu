@@ -585,13 +585,12 @@ __device__ __forceinline__ bool cloud_outside_warp(const PmPrim& P, const PmGrid
   return sqrt(nn.d2) - P.a > r;
 }
 
-// Starting candidate of a warp search: the best of the stored nearest points of the 8 fine-cell
-// centres around q (lanes 0-7, one centre each), shared by the warp.  (INFINITY, -1) if none.
-__device__ __forceinline__ NNResult32 field_corner_candidate(const PmGridDev& G, float qx, float qy, float qz) {
-  const unsigned FULL = 0xffffffffu;
+// Starting candidate of a warp search, in two steps so that the load can be issued early: the field
+// record (nearest point and index) of one of the 8 fine-cell centres around q on lanes 0-7 (index -1
+// elsewhere and outside the grid), then the best of them shared by the warp ((INFINITY, -1) if none).
+__device__ __forceinline__ float4 field_corner_record(const PmGridDev& G, float qx, float qy, float qz) {
   const int lane = threadIdx.x & 31;
-  float d2 = INFINITY;
-  int idx = -1;
+  float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
   if (lane < 8 && G.n_points > 0) {
     const float inv = G.inv_cell32;
     const float qa[3] = {qx, qy, qz};
@@ -603,15 +602,18 @@ __device__ __forceinline__ NNResult32 field_corner_candidate(const PmGridDev& G,
       ok = ok && t >= 0.f && t <= (float)(nc[a] - 1);
       cc[a] = ok ? (int)t : 0;
     }
-    if (ok) {
-      const int2 nn = __ldg(G.cell_nn + cc[0] + nc[0] * (cc[1] + nc[1] * cc[2]));
-      if (nn.y >= 0) {
-        d2 = point_d2_32(G, nn.y, qx, qy, qz);
-        idx = nn.y;
-      }
-    }
+    if (ok) rec = __ldg(G.cell_np + cc[0] + nc[0] * (cc[1] + (int64_t)nc[1] * cc[2]));
   }
-  unsigned long long key = idx >= 0 ? nn_key(d2, idx) : ~0ull;
+  return rec;
+}
+__device__ __forceinline__ NNResult32 field_corner_candidate(const float4& rec, float qx, float qy, float qz) {
+  const unsigned FULL = 0xffffffffu;
+  const int idx = __float_as_int(rec.w);
+  unsigned long long key = ~0ull;
+  if (idx >= 0) {  // the FP32 expression of every walk (point_d2_32)
+    const float dx = rec.x - qx, dy = rec.y - qy, dz = rec.z - qz;
+    key = nn_key(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), idx);
+  }
   for (int o = 4; o > 0; o >>= 1) {
     const unsigned long long k2 = __shfl_xor_sync(FULL, key, o);
     key = k2 < key ? k2 : key;
@@ -811,13 +813,14 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       float g, sd, mag;
       if (Pr.kind == PM_SDF_CLOUD) {
         const PmGridDev& Gc = v.C[Pr.cloud];
-        const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z);
+        const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z, !want_dist && check);
         const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
         if (fb.lb - Pr.a - S.r > margin32(qmag + fb.lb) + ek + (want_dist ? cutoff : 0.f)) continue;
         if (!want_dist && check && fb.idx >= 0) {
           // the centre's nearest point is a real point: if it is certainly within reach, the
           // sphere collides and no search is needed
-          const float ub = sqrtf(point_d2_32(Gc, fb.idx, sc.x, sc.y, sc.z));
+          const float ex = fb.np.x - sc.x, ey = fb.np.y - sc.y, ez = fb.np.z - sc.z;
+          const float ub = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez)));
           if (ub - Pr.a - S.r < -(margin32(qmag + ub) + ek)) {
             fail = 1;
             break;
@@ -909,54 +912,78 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     }
   }
   __syncthreads();
-  // ---- 3b. queued cloud queries, one warp per query
+  // ---- 3b. queued cloud queries, one warp per query; the next query's field records are read
+  //          before the current query's walk, so their latency hides behind it
   {
     const int lane = tid & 31;
     const int nq = min(sm.hq_n[0], hq_cap);
-    for (;;) {
+    auto pop = [&]() {
       int k = 0;
       if (lane == 0) k = atomicAdd(&sm.hq_n[1], 1);
-      k = __shfl_sync(0xffffffffu, k, 0);
-      if (k >= nq) break;
+      return __shfl_sync(FULL, k, 0);
+    };
+    auto centre = [&](int k) {  // the queried sphere's centre
+      const int2 e = sm.hq[k];
+      const int c = e.x / ns, si = e.x - c * ns;
+      const SphereF S = sm.sph[si];
+      const float* P = sm.pose + ((size_t)c * nsl + sm.grp[S.group].slot) * kPoseF;
+      return xf(P, S.x, S.y, S.z);
+    };
+    int k = pop();
+    float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    if (k < nq) {
+      const float3 q = centre(k);
+      rec = field_corner_record(v.C[sm.prm[sm.hq[k].y].cloud], q.x, q.y, q.z);
+    }
+    while (k < nq) {
+      const int kn = pop();
+      float4 rec_n = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+      if (kn < nq) {
+        const float3 q = centre(kn);
+        rec_n = field_corner_record(v.C[sm.prm[sm.hq[kn].y].cloud], q.x, q.y, q.z);
+      }
       const int2 e = sm.hq[k];
       const int c = e.x / ns, si = e.x - c * ns;
       const SphereF S = sm.sph[si];
       const GroupF& G = sm.grp[S.group];
       const bool check = !G.only_self;
       // warp-uniform: flags change under other warps, so lane 0 decides for the warp
-      const int done_c = __shfl_sync(0xffffffffu, (!want_dist && (sm.flags[c] & FLAG_FAIL)) ? 1 : 0, 0);
-      if (done_c) continue;
-      const PrimF& Pr = sm.prm[e.y];
-      const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
-      const float3 sc = xf(P, S.x, S.y, S.z);
-      const float ek = P[12] + P[13] * S.sn;
-      const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
-      const float reach = Pr.a + S.r + (want_dist ? m + cutoff : m);
-      const PmGridDev& Gc = v.C[Pr.cloud];
-      const NNResult32 start = field_corner_candidate(Gc, sc.x, sc.y, sc.z);
-      const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, start.d2, start.idx);
-      if (lane == 0) {
-        float g, sd, mag;
-        if (nn.idx < 0) {
-          g = reach - Pr.a - S.r;
-          sd = 3.0e38f;
-          mag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
-        } else {
-          const float d = sqrtf(nn.d2);
-          g = d - Pr.a - S.r;
-          sd = g;
-          mag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z) + d;
-        }
-        if (want_dist) atomicMin(&sm.sdist[c * ns + si], f2o(sd));
-        if (check) {
-          const float mm = margin32(mag) + ek;
-          if (g < -mm) {
-            atomicOr(&sm.flags[c], FLAG_FAIL);
-          } else if (g <= mm) {
-            push_item(scr, src, (int)(c0 + c), e.y << 1, si, nn.idx);
+      const int done_c = __shfl_sync(FULL, (!want_dist && (sm.flags[c] & FLAG_FAIL)) ? 1 : 0, 0);
+      if (!done_c) {
+        const PrimF& Pr = sm.prm[e.y];
+        const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
+        const float3 sc = xf(P, S.x, S.y, S.z);
+        const float ek = P[12] + P[13] * S.sn;
+        const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
+        const float reach = Pr.a + S.r + (want_dist ? m + cutoff : m);
+        const PmGridDev& Gc = v.C[Pr.cloud];
+        const NNResult32 start = field_corner_candidate(rec, sc.x, sc.y, sc.z);
+        const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, start.d2, start.idx);
+        if (lane == 0) {
+          float g, sd, mag;
+          if (nn.idx < 0) {
+            g = reach - Pr.a - S.r;
+            sd = 3.0e38f;
+            mag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
+          } else {
+            const float d = sqrtf(nn.d2);
+            g = d - Pr.a - S.r;
+            sd = g;
+            mag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z) + d;
+          }
+          if (want_dist) atomicMin(&sm.sdist[c * ns + si], f2o(sd));
+          if (check) {
+            const float mm = margin32(mag) + ek;
+            if (g < -mm) {
+              atomicOr(&sm.flags[c], FLAG_FAIL);
+            } else if (g <= mm) {
+              push_item(scr, src, (int)(c0 + c), e.y << 1, si, nn.idx);
+            }
           }
         }
       }
+      k = kn;
+      rec = rec_n;
     }
   }
   __syncthreads();

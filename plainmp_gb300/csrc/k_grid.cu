@@ -220,7 +220,7 @@ __global__ void k_edf_final(const int16_t* __restrict__ in, int64_t n, uint8_t* 
 // `reach` and a lower bound on the centre's distance to every point (the FP32 value shrunk by the
 // rounding of d^2, of the square root and of the FP32 point coordinates).  Cells whose
 // box-to-box bound already reaches `reach` skip the search.
-__global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int2* __restrict__ out) {
+__global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int2* __restrict__ out, float4* __restrict__ out_np) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)ncx * ncy * ncz) return;
   const int cx = (int)(i % ncx), cy = (int)((i / ncx) % ncy), cz = (int)(i / ((int64_t)ncx * ncy));
@@ -237,6 +237,12 @@ __global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int
     }
   }
   out[i] = make_int2(__float_as_int(fmaxf(d * (1.0f - 1e-6f) - slack, 0.0f)), idx);
+  float4 np = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+  if (idx >= 0) {
+    np = G.p32[idx];
+    np.w = __int_as_float(idx);
+  }
+  out_np[i] = np;
 }
 
 // Per-block candidate lists.  For a block whose cells all have a nearest point in the field, a
@@ -391,6 +397,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   uint8_t* edf = nullptr;
   float* cell_lb = nullptr;
   int2* cell_nn = nullptr;
+  float4* cell_np = nullptr;
   int2* blk_list = nullptr;
   int2* blk_cand = nullptr;
   float* blk_reach = nullptr;
@@ -464,6 +471,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
     {  // nearest-point field (needs the finished descriptor for its nearest-neighbour walks)
       const int64_t ncl = (int64_t)nc[0] * nc[1] * nc[2];
       if ((e = keep(ncl * 8, (void**)&cell_nn)) != cudaSuccess) break;
+      if ((e = keep(ncl * 16, (void**)&cell_np)) != cudaSuccess) break;
       PmGridDev v = d;
       v.blk_list = nullptr;  // the walks below run without candidate lists
       v.blk_cand = nullptr;
@@ -479,10 +487,11 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       v.edf = edf;
       v.cell_lb = cell_lb;
       v.n_points = (int32_t)n;
-      k_field<<<nblk(ncl, 128), 128, 0, s>>>(v, nc[0], nc[1], nc[2], (float)g.field_reach, cell_nn);
+      k_field<<<nblk(ncl, 128), 128, 0, s>>>(v, nc[0], nc[1], nc[2], (float)g.field_reach, cell_nn, cell_np);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
       // per-block candidate lists
       v.cell_nn = cell_nn;
+      v.cell_np = cell_np;
       int32_t *cnt = nullptr, *lstart = nullptr;
       if ((e = keep(nblocks * 4, (void**)&blk_reach)) != cudaSuccess) break;
       if ((e = keep(nblocks * 8, (void**)&blk_list)) != cudaSuccess) break;
@@ -519,6 +528,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.edf = edf;
   d.cell_lb = cell_lb;
   d.cell_nn = cell_nn;
+  d.cell_np = cell_np;
   d.blk_list = blk_list;
   d.blk_cand = blk_cand;
   d.blk_reach = blk_reach;

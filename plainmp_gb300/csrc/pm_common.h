@@ -83,6 +83,8 @@ struct PmGridDev {
   const int2* cell_nn;     // per fine cell (x fastest): x = lower bound (m, float bits) on the distance from the
                            // cell centre to any point, y = sorted index of the centre's nearest point (-1: none
                            // within field_reach)
+  const float4* cell_np;   // per fine cell: that nearest point itself (x y z as p32, w = its index as int
+                           // bits, -1: none), so a query reads point and index in one load
   float field_reach;       // cell_nn searched up to this distance from each centre
   int32_t pad_nn;
   const int2* blk_list;    // per block: [first, end) of its candidate list in blk_cand (first = -1: none)

@@ -230,12 +230,14 @@ __device__ __forceinline__ float field_centre(float origin, int c, float cellf) 
 // would do; the containing one is the tightest); idx = the nearest point of that centre, an upper
 // bound candidate (-1 if none within field_reach, and outside the grid).  Outside the grid, lb is
 // the distance to the box of the points.
+// With want_np, np = that point's record (x y z, w = index bits), read in parallel with the bound.
 struct FieldLB {
   float lb;
   int idx;
+  float4 np;
 };
-__device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, float qy, float qz) {
-  FieldLB f{INFINITY, -1};
+__device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, float qy, float qz, bool want_np = false) {
+  FieldLB f{INFINITY, -1, make_float4(0.f, 0.f, 0.f, 0.f)};
   if (G.n_points <= 0) return f;
   const float cellf = G.cell32;
   const float inv = G.inv_cell32;
@@ -258,7 +260,9 @@ __device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, fl
     f.lb = fmaxf(sqrtf(d2) * (1.0f - 1e-6f) - 4e-6f, 0.f);
     return f;
   }
-  const int2 nn = __ldg(G.cell_nn + cc[0] + nc[0] * (cc[1] + nc[1] * cc[2]));
+  const int64_t ci = cc[0] + nc[0] * (cc[1] + (int64_t)nc[1] * cc[2]);
+  const int2 nn = __ldg(G.cell_nn + ci);
+  if (want_np) f.np = __ldg(G.cell_np + ci);
   const float dx = qx - field_centre(G.o32[0], cc[0], cellf), dy = qy - field_centre(G.o32[1], cc[1], cellf),
               dz = qz - field_centre(G.o32[2], cc[2], cellf);
   const float off = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * (1.0f + 1e-6f) + 1e-7f;
