@@ -322,8 +322,10 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
       bal &= bal - 1;
       const int c0 = __shfl_sync(FULL, occ.x, src), c1 = __shfl_sync(FULL, occ.y, src);
       for (int c = c0 + lane; c < c1; c += 32) {
-        if (box_d2_32(G.cell_box + 6 * c, qx, qy, qz) >= best) continue;
-        const int2 pr = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + c);
+        const float4 lo = __ldg(G.cell_rec + 2 * c), hi = __ldg(G.cell_rec + 2 * c + 1);
+        const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+        if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) >= best) continue;
+        const int2 pr = make_int2(__float_as_int(lo.w), __float_as_int(hi.w));
         for (int p = pr.x; p < pr.y; p++) {
           const float4 pt = __ldg(G.p32 + p);
           const float dx = pt.x - qx, dy = pt.y - qy, dz = pt.z - qz;
@@ -386,12 +388,16 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
             const int own_first = __shfl_sync(FULL, occ.x, lo), own_excl = __shfl_sync(FULL, incl - n, lo);
             cs[j] = t < total ? own_first + (t - own_excl) : -1;
           }
+          // box and point range of each cell in one record: one round trip instead of two
           int2 pr[4];
 #pragma unroll
           for (int j = 0; j < 4; j++) {
             pr[j] = make_int2(0, 0);
-            if (cs[j] >= 0 && box_d2_32(G.cell_box + 6 * cs[j], qx, qy, qz) < best)
-              pr[j] = __ldg(reinterpret_cast<const int2*>(G.cell_pts) + cs[j]);
+            if (cs[j] >= 0) {
+              const float4 lo = __ldg(G.cell_rec + 2 * cs[j]), hi = __ldg(G.cell_rec + 2 * cs[j] + 1);
+              const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+              if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < best) pr[j] = make_int2(__float_as_int(lo.w), __float_as_int(hi.w));
+            }
           }
 #pragma unroll
           for (int j = 0; j < 4; j++) {
@@ -645,7 +651,7 @@ __device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int 
 
 struct Smem {
   double* qbuf;  // generated configurations (edges)
-  int2* hq;      // hard cloud queries: (cfg * n_spheres + sphere, primitive)
+  int2* hq;      // hard cloud queries: (cfg << 16 | sphere, primitive)
   int* hq_n;     // [0] pushed, [1] popped
   int* sdist;    // per (cfg, sphere): running minimum signed distance, order-preserving int
   float* pose;   // [cfg][slot][kPoseF]
@@ -828,7 +834,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         }
         const int k = atomicAdd(&sm.hq_n[0], 1);
         if (k < hq_cap) {
-          sm.hq[k] = make_int2(c * ns + si, p);
+          sm.hq[k] = make_int2(c << 16 | si, p);
           continue;
         }
         clearance(Pr, v.C, sc.x, sc.y, sc.z, S.r, S.tiny, want_dist ? m + cutoff : m, g, sd, mag);
@@ -924,7 +930,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     };
     auto centre = [&](int k) {  // the queried sphere's centre
       const int2 e = sm.hq[k];
-      const int c = e.x / ns, si = e.x - c * ns;
+      const int c = e.x >> 16, si = e.x & 0xffff;
       const SphereF S = sm.sph[si];
       const float* P = sm.pose + ((size_t)c * nsl + sm.grp[S.group].slot) * kPoseF;
       return xf(P, S.x, S.y, S.z);
@@ -943,7 +949,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         rec_n = field_corner_record(v.C[sm.prm[sm.hq[kn].y].cloud], q.x, q.y, q.z);
       }
       const int2 e = sm.hq[k];
-      const int c = e.x / ns, si = e.x - c * ns;
+      const int c = e.x >> 16, si = e.x & 0xffff;
       const SphereF S = sm.sph[si];
       const GroupF& G = sm.grp[S.group];
       const bool check = !G.only_self;

@@ -97,7 +97,7 @@ __global__ void k_flags(const int32_t* __restrict__ count, int64_t nc, int32_t* 
 
 __global__ void k_cell_records(const int32_t* __restrict__ count, const int32_t* __restrict__ start, const int32_t* __restrict__ recidx,
                                int64_t nc, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
-                               float* __restrict__ cell_box, int32_t* __restrict__ cell_pts) {
+                               float* __restrict__ cell_box, int32_t* __restrict__ cell_pts, float4* __restrict__ cell_rec) {
   int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= nc || count[c] == 0) return;
   int r = recidx[c];
@@ -116,6 +116,8 @@ __global__ void k_cell_records(const int32_t* __restrict__ count, const int32_t*
   }
   cell_pts[2 * r] = p0;
   cell_pts[2 * r + 1] = p1;
+  cell_rec[2 * r] = make_float4(cell_box[6 * r], cell_box[6 * r + 1], cell_box[6 * r + 2], __int_as_float(p0));
+  cell_rec[2 * r + 1] = make_float4(cell_box[6 * r + 3], cell_box[6 * r + 4], cell_box[6 * r + 5], __int_as_float(p1));
 }
 
 __global__ void k_block_records(const int32_t* __restrict__ recidx_ex, int64_t nblocks, int32_t n_rec, const float* __restrict__ cell_box,
@@ -398,6 +400,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   float* cell_lb = nullptr;
   int2* cell_nn = nullptr;
   float4* cell_np = nullptr;
+  float4* cell_rec = nullptr;
   int2* blk_list = nullptr;
   int2* blk_cand = nullptr;
   float* blk_reach = nullptr;
@@ -438,7 +441,8 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
     n_rec = last_idx + last_flag;
     if ((e = keep((size_t)n_rec * 24, (void**)&cell_box)) != cudaSuccess) break;
     if ((e = keep((size_t)n_rec * 8, (void**)&cell_pts)) != cudaSuccess) break;
-    k_cell_records<<<nblk(ncells, 256), 256, 0, s>>>(count, start, recidx, ncells, px, py, pz, cell_box, cell_pts);
+    if ((e = keep((size_t)std::max<int32_t>(n_rec, 1) * 32, (void**)&cell_rec)) != cudaSuccess) break;
+    k_cell_records<<<nblk(ncells, 256), 256, 0, s>>>(count, start, recidx, ncells, px, py, pz, cell_box, cell_pts, cell_rec);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     k_block_records<<<nblk(nblocks, 128), 128, 0, s>>>(recidx, nblocks, n_rec, cell_box, blk_occ, blk_box);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
@@ -484,6 +488,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       v.blk_box = blk_box;
       v.cell_box = cell_box;
       v.cell_pts = cell_pts;
+      v.cell_rec = cell_rec;
       v.edf = edf;
       v.cell_lb = cell_lb;
       v.n_points = (int32_t)n;
@@ -525,6 +530,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.blk_box = blk_box;
   d.cell_box = cell_box;
   d.cell_pts = cell_pts;
+  d.cell_rec = cell_rec;
   d.edf = edf;
   d.cell_lb = cell_lb;
   d.cell_nn = cell_nn;

@@ -78,6 +78,8 @@ struct PmGridDev {
   const float* blk_box;    // per block: lo xyz, hi xyz (empty: +inf/-inf)
   const float* cell_box;   // per occupied cell: lo xyz, hi xyz
   const int32_t* cell_pts; // per occupied cell: [first point, end)
+  const float4* cell_rec;  // per occupied cell, both in one 32-byte record: (lo xyz, first point as int
+                           // bits), (hi xyz, end as int bits)
   const uint8_t* edf;      // per block: Chebyshev distance in blocks to the nearest occupied block (capped at 255)
   const float* cell_lb;    // per fine cell (x fastest): lower bound (m) on the distance from the cell to any point
   const int2* cell_nn;     // per fine cell (x fastest): x = lower bound (m, float bits) on the distance from the
