@@ -288,6 +288,10 @@ int pmgpu_traj_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, co
  * returns the summed device time (ms) and launch count of the named kernel since the last
  * read ("*" = all kernels) and clears them.  No counterpart in the reference. */
 int pmgpu_profile_enable(int on);
+/* Measured FMA throughput of this GPU (TFLOP/s, 2 flops per FMA): fp64 = 0 for FP32, 1 for FP64.
+ * Runs a short microbenchmark kernel on the stream and synchronises.  The denominator of the
+ * rooflines of arithmetic-bound kernels.  No counterpart in the reference. */
+int pmgpu_measure_fma_peak(int fp64, double* tflops, void* stream);
 int pmgpu_profile_read(const char* kernel, double* total_ms, int64_t* launches);
 
 #ifdef __cplusplus

@@ -115,6 +115,7 @@ _SIGS = {
     "pmgpu_traj_cost": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p, _i, _p]),
     "pmgpu_profile_enable": (_i, [_i]),
     "pmgpu_profile_read": (_i, [C.c_char_p, _dp, _i64p]),
+    "pmgpu_measure_fma_peak": (_i, [_i, _dp, _p]),
 }
 
 for _name, (_res, _args) in _SIGS.items():
@@ -148,6 +149,13 @@ def profile_read(kernel: str = "*"):
     n = C.c_int64(0)
     check(lib.pmgpu_profile_read(kernel.encode(), C.byref(ms), C.byref(n)))
     return float(ms.value), int(n.value)
+
+
+def measure_fma_peak(fp64: bool = False, stream=None) -> float:
+    """Measured FMA throughput of the current GPU in TFLOP/s (FP32, or FP64 with fp64=True)."""
+    t = C.c_double(0.0)
+    check(lib.pmgpu_measure_fma_peak(int(bool(fp64)), C.byref(t), stream))
+    return float(t.value)
 
 
 def device_count() -> int:

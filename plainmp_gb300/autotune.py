@@ -13,7 +13,7 @@ import os
 from pathlib import Path
 from typing import Optional, Tuple
 
-SHAPES = [(16, 128), (32, 128), (32, 256), (64, 256), (32, 512), (64, 512), (128, 512)]
+SHAPES = [(16, 128), (32, 128), (16, 256), (32, 256), (64, 256), (32, 512), (64, 512), (128, 512)]
 
 
 def cache_path() -> Path:

@@ -1622,7 +1622,7 @@ extern "C" {
 int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block) {
   return guarded([&] {
     check_ptr(c, "cst");
-    static const int ok[][2] = {{16, 128}, {32, 128}, {32, 256}, {64, 256}, {32, 512}, {64, 512}, {128, 512}};
+    static const int ok[][2] = {{16, 128}, {32, 128}, {16, 256}, {32, 256}, {64, 256}, {32, 512}, {64, 512}, {128, 512}};
     bool found = false;
     for (auto& p : ok) found = found || (p[0] == configs_per_block && p[1] == threads_per_block);
     if (!found) throw std::invalid_argument("unsupported (configs_per_block, threads_per_block) pair");
@@ -2105,6 +2105,36 @@ int pmgpu_posecst_is_valid(pmgpu_posecst* c, const double* q, int64_t B, uint8_t
       stage_out(out, dout, (size_t)B, s);
       cuda_check(cudaStreamSynchronize(s), "pose constraint is_valid");
     }
+  });
+}
+
+int pmgpu_measure_fma_peak(int fp64, double* tflops, void* stream) {
+  return guarded([&] {
+    check_ptr(tflops, "tflops");
+    cudaStream_t s = as_stream(stream);
+    int dev = 0, n_sm = 0;
+    cuda_check(cudaGetDevice(&dev), "device");
+    cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "device");
+    const int threads = 256, blocks = n_sm * 8;  // 64 warps per SM: every scheduler has work
+    const int iters = fp64 ? 512 : 8192;
+    DevBuf out;
+    out.ensure((size_t)blocks * threads * 8);
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    float best = 0.f;
+    for (int r = 0; r < 6; r++) {  // the first launch warms up; the best of the rest counts
+      cuda_check(cudaEventRecord(e0, s), "event");
+      cuda_check(launch_fma_peak(fp64, iters, out.p, blocks, threads, s), "fma_peak");
+      cuda_check(cudaEventRecord(e1, s), "event");
+      cuda_check(cudaEventSynchronize(e1), "event");
+      float ms = 0.f;
+      cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
+      if (r > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = 16.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   });
 }
 

@@ -1369,6 +1369,7 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   bool launched = false;
   PM_FAST_CASE(16, 128)
   PM_FAST_CASE(32, 128)
+  PM_FAST_CASE(16, 256)
   PM_FAST_CASE(32, 256)
   PM_FAST_CASE(64, 256)
   PM_FAST_CASE(32, 512)

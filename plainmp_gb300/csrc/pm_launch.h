@@ -83,6 +83,10 @@ cudaError_t launch_sdf_points(const PmPrim* prims, int n_prims, const PmGridDev*
 cudaError_t launch_cloud_nearest(const PmGridDev* grid, const double* pts, int64_t n, double* sq, double* near3,
                                  cudaStream_t s);
 
+// ---- FMA throughput microbenchmark (k_peak.cu): blocks x threads threads, 16 flops per iteration
+// each; out receives blocks * threads values of the element type (double when fp64).
+cudaError_t launch_fma_peak(int fp64, int iters, void* out, int blocks, int threads, cudaStream_t s);
+
 // ---- point-cloud grid build (k_grid.cu)
 struct GridBuild {
   // inputs

@@ -234,3 +234,44 @@ def test_fast_edges_degenerate(chain):
     ref, _ = oc.check_motion(s1, s2, 0, w)
     assert np.array_equal(got, ref)
     assert got[:4].all()
+
+
+def test_fast_every_launch_shape(dual):
+    """Every (configs per block, threads) pair the autotuner may pick gives the same validity and
+    the same FP32 distances: the shape changes the work split, never the arithmetic."""
+    from plainmp_gb300._lib import CudaError
+    from plainmp_gb300.autotune import SHAPES
+
+    (_, cst, _), (_, oc, _) = dual
+    Q = W.dualarm_configs(777, seed=21)  # a ragged last block for every shape
+    ref = oc.is_valid(Q, threads=8)
+    keep = cst.get_fast_launch()
+    ran = 0
+    try:
+        d0 = None
+        for cpb, nt in SHAPES:
+            cst.set_fast_launch(cpb, nt)
+            try:
+                ok, d = cst.is_valid_fast(Q, distances=True)
+            except CudaError as e:  # the block's tables do not fit in shared memory at this shape
+                assert "invalid configuration" in str(e), (cpb, nt, str(e))
+                continue
+            ran += 1
+            assert np.array_equal(ok, ref), (cpb, nt)
+            if d0 is None:
+                d0 = d
+            assert np.array_equal(d, d0), (cpb, nt)
+    finally:
+        cst.set_fast_launch(*keep)
+    assert ran >= 5, ran
+
+
+def test_fma_peak_microbenchmark():
+    """The measured FMA throughput used as the roofline denominator is in a plausible range for
+    this GPU (FP32 tens of TFLOP/s, FP64 at least a fraction of a TFLOP/s and below FP32)."""
+    from plainmp_gb300 import _lib
+
+    f32 = _lib.measure_fma_peak(False)
+    f64 = _lib.measure_fma_peak(True)
+    assert 10.0 < f32 < 400.0, f32
+    assert 0.05 < f64 < f32, (f64, f32)
