@@ -232,6 +232,60 @@ def _capture(fn):
     return g
 
 
+def ik_grad_check(cst, link, q, tgt, dev, h=1e-6, w_rot=0.1, margin=0.02):
+    """Max relative error of the FP32 adjoint gradient of the C3 cost on a sample of problems, against
+    central differences (h = 1e-6, FP64) of the same cost evaluated in FP64 by the library's plain
+    device method (sin/cos FK link pose, exact per-sphere SDF distances).  Error per problem:
+    |g - g_fd|_inf / max(1, |g_fd|_inf); problems where differences at h and h/2 disagree (a hinge
+    switching inside the step) are left out, as in the gradient tests."""
+    import torch
+
+    from plainmp_gb300 import diff
+
+    if cst.groups()["only_self"].any():  # the hinge would need the active-sphere mask
+        return None
+    q32 = torch.tensor(q, dtype=torch.float32, device=dev)
+    Q = q32.double()  # the FD runs at exactly the FP32 point the kernel sees
+    T = tgt.double()
+
+    def qmul(a, b):
+        ax, ay, az, aw = a.unbind(-1)
+        bx, by, bz, bw = b.unbind(-1)
+        return torch.stack([aw * bx + ax * bw + ay * bz - az * by, aw * by + ay * bw + az * bx - ax * bz,
+                            aw * bz + az * bw + ax * by - ay * bx, aw * bw - ax * bx - ay * by - az * bz], -1)
+
+    def cost64(P, Tr):
+        pose = diff.link_poses(cst, P, link)
+        c = ((pose[:, :3] - Tr[:, :3]) ** 2).sum(1)
+        e = qmul(Tr[:, 3:] * torch.tensor([-1.0, -1.0, -1.0, 1.0], dtype=torch.float64, device=dev), pose[:, 3:])
+        e = torch.where(e[:, 3:4] < 0, -e, e)
+        sn = e[:, :3].norm(dim=1)
+        k = torch.where(sn > 1e-12, 2.0 * torch.atan2(sn, e[:, 3]) / sn.clamp_min(1e-300), 2.0 / e[:, 3])
+        c = c + w_rot * ((k[:, None] * e[:, :3]) ** 2).sum(1)
+        d = torch.as_tensor(cst.sphere_distances(P, high_accuracy=True), device=dev)
+        return c + (torch.clamp(margin - d, min=0.0) ** 2).sum(1)
+
+    def fd(step):
+        B, d = Q.shape
+        P = Q[:, None, :].repeat(1, 2 * d, 1)
+        for j in range(d):
+            P[:, 2 * j, j] += step
+            P[:, 2 * j + 1, j] -= step
+        v = cost64(P.reshape(-1, d), T.repeat_interleave(2 * d, dim=0)).reshape(B, 2 * d)
+        return (v[:, 0::2] - v[:, 1::2]) / (2 * step)
+
+    def rel(g, ref):
+        return (g - ref).abs().amax(1) / ref.abs().amax(1).clamp_min(1.0)
+
+    g1, g2 = fd(h), fd(h / 2)
+    keep = rel(g1, g2) < 1e-5
+    _, g = diff.ik_cost_grad(cst, q32, tgt, link)
+    err = rel(g.double(), g1)[keep]
+    return {"problems": int(Q.shape[0]), "smooth": int(keep.sum()), "max_rel_err": float(err.max()) if err.numel() else None,
+            "tolerance": 1e-4,
+            "reference": "central differences (h = 1e-6) of the cost in FP64 by the plain device method"}
+
+
 def bench_ik(dev, timed, steps=50, lr=0.05, fp32_peak=None):
     """C3: 8192 collision-aware IK problems on the C0 chain and scene, `steps` gradient steps
     each.  One gradient eval = cost + adjoint gradient of one problem at one step."""
@@ -271,6 +325,7 @@ def bench_ik(dev, timed, steps=50, lr=0.05, fp32_peak=None):
     except Exception as e:  # noqa: BLE001 - reported in the JSON line
         ms_graph = None
         graph_err = f"{type(e).__name__}: {e}"
+    grad_check = ik_grad_check(cst, link, q0[:64], tgt[:64], dev)
     evals = n * steps
     # algorithmic flops per eval (no broad phase, no early exit): forward FK 7 x 90 + 8 links x 24,
     # 56 sphere transforms x 18, narrow phase 56 x (35 x 10 boxes + 11 x 5 spheres + 30 x 5
@@ -287,6 +342,7 @@ def bench_ik(dev, timed, steps=50, lr=0.05, fp32_peak=None):
         "autograd_cuda_graph": evals / (ms_graph / 1e3) if ms_graph else None,
         "ms": {"fused_descent": ms_fused, "autograd_eager": ms_eager, "autograd_cuda_graph": ms_graph},
         "median_cost": {"initial": float(c_init.median()), "after_descent": float(c_final.median())},
+        "gradient_check": grad_check,
         "roofline": {"bound": "fp32 issue", "achieved": achieved, "peak": fp32_peak or FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                      "frac": achieved / (fp32_peak or FP32_NOMINAL_TFLOPS),
                      "peak_kind": "measured (FP32 FMA microbenchmark k_fma_peak)" if fp32_peak else "nominal (FP32 FMA, 2.07 GHz)",
@@ -519,14 +575,14 @@ def main():
         traffic, issue = pj.get("dram_bytes_per_launch"), pj.get("issue_active_pct")
 
     side = None
-    peaks = None
+    fma_peaks = None
     if rank == 0 and not args.headline_only:
         # measured FMA throughput of this GPU: the denominator of the arithmetic-bound rooflines
-        peaks = {"fp32_fma_tflops": _lib.measure_fma_peak(False), "fp64_fma_tflops": _lib.measure_fma_peak(True),
+        fma_peaks = {"fp32_fma_tflops": _lib.measure_fma_peak(False), "fp64_fma_tflops": _lib.measure_fma_peak(True),
                  "how": "k_fma_peak: 8 independent FMA chains per thread, 64 warps per SM, best of 5 launches (CUDA events)"}
         timed2 = _timer(dev, flush, stream)
         side = bench_chain7(dev, timed2)
-        side["C3"] = bench_ik(dev, timed2, fp32_peak=peaks["fp32_fma_tflops"])
+        side["C3"] = bench_ik(dev, timed2, fp32_peak=fma_peaks["fp32_fma_tflops"])
         side["C4"] = bench_traj(dev, timed2)
 
     if rank != 0:
@@ -563,8 +619,8 @@ def main():
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
-    if peaks is not None:
-        line["measured_peaks"] = peaks
+    if fma_peaks is not None:
+        line["measured_peaks"] = fma_peaks
     if side is not None:
         line["workloads"] = side
     print(json.dumps(line), flush=True)
