@@ -601,7 +601,8 @@ def main():
         "vs_baseline": None,
         "dtype": "f32 (FP64 FK and FP64 recheck of uncertain decisions)",
         "data": "synthetic (seeded generators in plainmp_gb300/workloads.py)",
-        "config": config_dict({"launch_shape": {"with_distances": list(shape_dist), "validity_only": list(shape_valid)}}),
+        "config": config_dict({"launch_shape": {"with_distances": list(shape_dist), "validity_only": list(shape_valid)},
+                               "cloud_grid": sdf.stats()}),
         "e2e": {"value": e2e_value, "unit": "configs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": all_n,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

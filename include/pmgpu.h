@@ -109,6 +109,10 @@ int pmgpu_sdf_ground_create(double height, pmgpu_sdf** out);
  * uniform grid that answers exact nearest-neighbour queries in place of the KD-tree
  * (collision/kdtree.cpp:20-96).  cell_size <= 0 picks a size from the point density. */
 int pmgpu_sdf_cloud_create(const double* points, int64_t n, double radius, double cell_size, pmgpu_sdf** out);
+/* Sizes of a cloud's device grid (built on first call if needed): out6 = {points, occupied fine
+ * cells, blocks, fine cells of the nearest-point field, candidate-list entries, device bytes}.
+ * No counterpart in the reference (its KD-tree lives in host memory). */
+int pmgpu_sdf_cloud_stats(pmgpu_sdf* sdf, int64_t* out6);
 /* UnionSDF(members): members are shared, not copied (primitive_sdf.hpp:102) */
 int pmgpu_sdf_union_create(pmgpu_sdf* const* members, int n, pmgpu_sdf** out);
 /* UnionSDF.add / merge (primitive_sdf.hpp:115-133): clone=1 deep-copies */

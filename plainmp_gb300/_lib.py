@@ -77,6 +77,7 @@ _SIGS = {
     "pmgpu_sdf_sphere_create": (_i, [_d, _dp, _dp, C.POINTER(_p)]),
     "pmgpu_sdf_ground_create": (_i, [_d, C.POINTER(_p)]),
     "pmgpu_sdf_cloud_create": (_i, [_dp, _i64, _d, _d, C.POINTER(_p)]),
+    "pmgpu_sdf_cloud_stats": (_i, [_p, _i64p]),
     "pmgpu_sdf_union_create": (_i, [C.POINTER(_p), _i, C.POINTER(_p)]),
     "pmgpu_sdf_union_add": (_i, [_p, _p, _i]),
     "pmgpu_sdf_clone": (_i, [_p, C.POINTER(_p)]),

@@ -1233,6 +1233,24 @@ int pmgpu_sdf_ground_create(double height, pmgpu_sdf** out) {
     *out = wrap(s);
   });
 }
+int pmgpu_sdf_cloud_stats(pmgpu_sdf* sdf, int64_t* out6) {
+  return guarded([&] {
+    check_ptr(sdf, "sdf");
+    check_ptr(out6, "out");
+    if (!sdf->s || !sdf->s->cloud) throw std::invalid_argument("not a CloudSDF");
+    CloudData& cd = *sdf->s->cloud;
+    if (!cd.built) build_cloud(cd);
+    const PmGridDev& d = cd.g.dev;
+    const int64_t nblocks = (int64_t)d.nbx * d.nby * d.nbz;
+    out6[0] = (int64_t)(cd.pts.size() / 3);
+    out6[1] = cd.g.n_occupied;
+    out6[2] = nblocks;
+    out6[3] = nblocks * PM_GRID_CELLS_PER_BLOCK;
+    out6[4] = cd.g.n_cand;
+    out6[5] = cd.g.bytes;
+  });
+}
+
 int pmgpu_sdf_cloud_create(const double* points, int64_t n, double radius, double cell_size, pmgpu_sdf** out) {
   return guarded([&] {
     if (n < 0) throw std::invalid_argument("negative point count");

@@ -361,10 +361,14 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   std::vector<void*> tmp;
   cudaError_t e = cudaSuccess;
   g.n_allocs = 0;
+  g.bytes = 0;
   auto keep = [&](size_t bytes, void** p) -> cudaError_t {
     if (g.n_allocs >= (int)(sizeof(g.allocs) / sizeof(g.allocs[0]))) return cudaErrorMemoryAllocation;
     cudaError_t r = cudaMalloc(p, bytes < 16 ? 16 : bytes);
-    if (r == cudaSuccess) g.allocs[g.n_allocs++] = *p;
+    if (r == cudaSuccess) {
+      g.allocs[g.n_allocs++] = *p;
+      g.bytes += (int64_t)(bytes < 16 ? 16 : bytes);
+    }
     return r;
   };
   auto scratch = [&](size_t bytes, void** p) -> cudaError_t {
@@ -538,6 +542,8 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.blk_list = blk_list;
   d.blk_cand = blk_cand;
   d.blk_reach = blk_reach;
+  g.n_occupied = n_rec;
+  g.n_cand = n_cand;
   d.field_reach = (float)g.field_reach;
   d.n_points = (int32_t)n;
   return cudaSuccess;

@@ -99,6 +99,8 @@ struct GridBuild {
   PmGridDev dev;
   void* allocs[24];
   int n_allocs;
+  // sizes of what was built: occupied fine cells, candidate-list entries, device bytes kept
+  int64_t n_occupied = 0, n_cand = 0, bytes = 0;
 };
 // Builds the grid synchronously on `s` (allocates device memory); returns cudaSuccess or the
 // first CUDA error.  host_lb/host_ub receive the CloudSDF AABB.

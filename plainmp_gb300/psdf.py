@@ -188,6 +188,14 @@ class CloudSDF(PrimitiveSDFBase):
         check(lib.pmgpu_cloud_nearest(self._h, b.ptr, n, sp, npt, b.mem, b.stream))
         return sq, near
 
+    def stats(self) -> dict:
+        """Sizes of the device grid: points, occupied fine cells, blocks, field cells, candidate-list
+        entries and device bytes (the grid is built first if it is not yet)."""
+        out = np.zeros(6, dtype=np.int64)
+        check(lib.pmgpu_sdf_cloud_stats(self._h, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        keys = ("points", "occupied_cells", "blocks", "field_cells", "list_entries", "device_bytes")
+        return {k: int(v) for k, v in zip(keys, out)}
+
 
 class UnionSDF(SDFBase):
     def __init__(self, sdf_list: List[SDFBase]) -> None:

@@ -275,3 +275,17 @@ def test_fma_peak_microbenchmark():
     f64 = _lib.measure_fma_peak(True)
     assert 10.0 < f32 < 400.0, f32
     assert 0.05 < f64 < f32, (f64, f32)
+
+
+def test_cloud_stats():
+    """The grid's reported sizes are consistent with the cloud and with each other."""
+    from plainmp_gb300 import CloudSDF
+
+    pts = W.box_surface_cloud(n_points=20_000, seed=3)
+    st = CloudSDF(pts, 0.0).stats()
+    assert st["points"] == 20_000
+    assert 0 < st["occupied_cells"] <= st["points"]
+    assert st["field_cells"] == 64 * st["blocks"]
+    assert st["list_entries"] > 0
+    # at least the points (FP64 SoA + FP32) and the field (8 + 16 bytes per fine cell)
+    assert st["device_bytes"] >= 40 * st["points"] + 24 * st["field_cells"]
