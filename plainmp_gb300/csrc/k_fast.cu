@@ -356,13 +356,15 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
         int2 occ = make_int2(0, 0);
         int n = 0;
         bool beyond = true;  // this entry, and (sorted) every later one, lies beyond the best
-        if (k < rng.y) {
-          const int2 e = __ldg(G.blk_cand + k);
-          const float ed = __int_as_float(e.y);
+        if (k < rng.y) {  // the widened entry and its block's box: no dependent load
+          const int4 e = __ldg(G.cand4 + k);
+          const float4 lo = __ldg(G.cand_box + 2 * k), hi = __ldg(G.cand_box + 2 * k + 1);
+          const float ed = __int_as_float(e.w);
           beyond = ed * ed * (1.0f - 1e-5f) >= best;
           if (!beyond) {
-            occ = __ldg(reinterpret_cast<const int2*>(G.blk_occ) + e.x);
-            if (box_d2_32(G.blk_box + 6 * e.x, qx, qy, qz) < best) n = occ.y - occ.x;
+            occ = make_int2(e.x, e.y);
+            const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+            if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < best) n = occ.y - occ.x;
           }
         }
         const bool stop = __shfl_sync(FULL, beyond ? 1 : 0, 31) != 0;

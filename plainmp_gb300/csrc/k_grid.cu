@@ -328,6 +328,20 @@ __global__ void k_blk_lists(PmGridDev G, int pass, float reach_cap, float* __res
   if (pass == 0) cnt[b] = n;
 }
 
+// The candidate lists widened for the warp searches: each entry also carries its block's
+// occupied-cell range and box, read with the entry instead of one dependent load later.
+__global__ void k_cand_expand(const int2* __restrict__ cand, int64_t n, const int32_t* __restrict__ blk_occ,
+                              const float* __restrict__ blk_box, int4* __restrict__ cand4, float4* __restrict__ cand_box) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int2 e = cand[k];
+  const int b = e.x;
+  cand4[k] = make_int4(blk_occ[2 * b], blk_occ[2 * b + 1], b, e.y);
+  const float* x = blk_box + 6 * (int64_t)b;
+  cand_box[2 * k] = make_float4(x[0], x[1], x[2], 0.f);
+  cand_box[2 * k + 1] = make_float4(x[3], x[4], x[5], 0.f);
+}
+
 __global__ void k_blk_ranges(const float* __restrict__ R, const int32_t* __restrict__ cnt, const int32_t* __restrict__ start, int64_t nb,
                              int2* __restrict__ out) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -405,6 +419,8 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   int2* cell_nn = nullptr;
   float4* cell_np = nullptr;
   float4* cell_rec = nullptr;
+  int4* cand4 = nullptr;
+  float4* cand_box = nullptr;
   int2* blk_list = nullptr;
   int2* blk_cand = nullptr;
   float* blk_reach = nullptr;
@@ -517,6 +533,9 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       if ((e = keep((size_t)std::max<int32_t>(n_cand, 1) * 8, (void**)&blk_cand)) != cudaSuccess) break;
       k_blk_lists<<<nblk(nblocks, 128), 128, 0, s>>>(v, 1, (float)g.field_reach, blk_reach, cnt, lstart, blk_cand);
       k_blk_ranges<<<nblk(nblocks, 256), 256, 0, s>>>(blk_reach, cnt, lstart, nblocks, blk_list);
+      if ((e = keep((size_t)std::max<int32_t>(n_cand, 1) * 16, (void**)&cand4)) != cudaSuccess) break;
+      if ((e = keep((size_t)std::max<int32_t>(n_cand, 1) * 32, (void**)&cand_box)) != cudaSuccess) break;
+      if (n_cand > 0) k_cand_expand<<<nblk(n_cand, 256), 256, 0, s>>>(blk_cand, n_cand, blk_occ, blk_box, cand4, cand_box);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
     e = cudaStreamSynchronize(s);
@@ -542,6 +561,8 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.blk_list = blk_list;
   d.blk_cand = blk_cand;
   d.blk_reach = blk_reach;
+  d.cand4 = cand4;
+  d.cand_box = cand_box;
   g.n_occupied = n_rec;
   g.n_cand = n_cand;
   d.field_reach = (float)g.field_reach;

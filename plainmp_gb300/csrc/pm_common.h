@@ -93,6 +93,9 @@ struct PmGridDev {
   const int2* blk_cand;    // candidate lists: (occupied block, float bits of its box distance from the listing
                            // block's box), nearest first, within blk_reach
   const float* blk_reach;  // per block: a query in the block whose search bound is below this needs only its list
+  const int4* cand4;       // blk_cand widened for the warp searches: (first occupied-cell record, end, block,
+                           // float bits of the distance), so one load gives the cell range
+  const float4* cand_box;  // per list entry, its block's box: (lo xyz, 0), (hi xyz, 0)
   // FP32 copies for the FP32 queries (no FP64 arithmetic on their path): origin, block edge and
   // its reciprocal, fine cell edge and its reciprocal, and the points' box (rounded outwards)
   float o32[3], blk32, inv_blk32, cell32, inv_cell32;
