@@ -577,6 +577,31 @@ static std::vector<size_t> farthest_order(const std::vector<std::array<double, 3
   return visited;
 }
 
+// Two-stream pipeline of a host-memory fast call: chunk i runs on stream i % 2 (the caller's stream,
+// or an internal non-blocking one) with buffer set i % 2, so each chunk's copies overlap the
+// neighbouring chunks' kernels.  Chunks on the same stream run in order, so a buffer set is reused
+// only after the chunk before it on that stream has finished.
+struct FastPipe {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  DevBuf in[2], out[2], dist[2], items[2];
+  DevBuf ctl, ovf;  // per chunk counters (64 B each) and per-config overflow flags, for the whole call
+  FastPipe() = default;
+  FastPipe(const FastPipe&) = delete;
+  FastPipe& operator=(const FastPipe&) = delete;
+  ~FastPipe() {
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (aux) cudaStreamDestroy(aux);
+  }
+  void init() {
+    if (aux) return;
+    cuda_check(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking), "stream");
+    cuda_check(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming), "event");
+    cuda_check(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming), "event");
+  }
+};
+
 struct HostCst {
   std::shared_ptr<HostModel> kin;
   std::vector<int> ids;
@@ -598,6 +623,7 @@ struct HostCst {
   // workspaces for host-memory calls
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
+  FastPipe pipe;                      // host-memory fast calls of large batches
   DevBuf e_sr, e_n, e_off;            // fast edge path: step ratios, waypoint counts and offsets
   DevBuf g_wp;                        // trajectory costs: per-waypoint partial costs
   std::vector<int16_t> seq_host;
@@ -1655,6 +1681,61 @@ int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* t
     *threads_per_block = c->c.fast_nt;
   });
 }
+// Host-memory fast call of a large batch, in up to 8 chunks of at least 8,192 configurations on two
+// streams (FastPipe).  Every configuration is independent, so the outcome is the same as one launch.
+static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* st, const double* q, int64_t B, uint8_t* out,
+                                float* dist32, int64_t* stats, cudaStream_t s) {
+  FastPipe& P = C.pipe;
+  P.init();
+  const int64_t d = C.q_dim(), ns = C.n_spheres();
+  const int64_t n_chunks = std::max<int64_t>(2, std::min<int64_t>(8, B / 8192));
+  const int64_t chunk = ((B + n_chunks - 1) / n_chunks + 127) / 128 * 128;
+  const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(4 * chunk, 1 << 16), (int64_t)1 << 28);
+  char* ctl = (char*)P.ctl.ensure((size_t)n_chunks * 64);
+  uint8_t* ovf = (uint8_t*)P.ovf.ensure(std::max<size_t>((size_t)B, 16));
+  double* din[2];
+  uint8_t* dout[2];
+  float* ddist[2];
+  int4* items[2];
+  for (int k = 0; k < 2; k++) {  // sized once per call, before any chunk is in flight
+    din[k] = (double*)P.in[k].ensure((size_t)chunk * d * 8);
+    dout[k] = (uint8_t*)P.out[k].ensure(std::max<size_t>((size_t)chunk, 16));
+    ddist[k] = dist32 ? (float*)P.dist[k].ensure((size_t)chunk * ns * 4) : nullptr;
+    items[k] = (int4*)P.items[k].ensure((size_t)cap * sizeof(int4));
+  }
+  cuda_check(cudaMemsetAsync(ctl, 0, (size_t)n_chunks * 64, s), "memset");
+  cuda_check(cudaMemsetAsync(ovf, 0, std::max<size_t>((size_t)B, 16), s), "memset");
+  cuda_check(cudaEventRecord(P.ev_in, s), "event");  // the second stream starts after the caller's prior work
+  cuda_check(cudaStreamWaitEvent(P.aux, P.ev_in, 0), "event");
+  for (int64_t i = 0; i < n_chunks; i++) {
+    const int64_t c0 = i * chunk;
+    if (c0 >= B) break;
+    const int64_t n = std::min<int64_t>(chunk, B - c0);
+    const int k = (int)(i & 1);
+    cudaStream_t cs = k ? P.aux : s;
+    cuda_check(cudaMemcpyAsync(din[k], q + c0 * d, (size_t)(n * d) * 8, cudaMemcpyHostToDevice, cs), "H2D copy");
+    char* cc = ctl + i * 64;
+    cuda_check(launch_fast_valid(T, C.hdr, st, din[k], n, dout[k], ddist[k], 0.1f, items[k], (unsigned int*)cc, cap, ovf + c0,
+                                 (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs),
+               "is_valid_fast");
+    cuda_check(cudaMemcpyAsync(out + c0, dout[k], (size_t)n, cudaMemcpyDeviceToHost, cs), "D2H copy");
+    if (dist32) cuda_check(cudaMemcpyAsync(dist32 + c0 * ns, ddist[k], (size_t)(n * ns) * 4, cudaMemcpyDeviceToHost, cs), "D2H copy");
+  }
+  cuda_check(cudaEventRecord(P.ev_out, P.aux), "event");
+  cuda_check(cudaStreamWaitEvent(s, P.ev_out, 0), "event");
+  cuda_check(cudaStreamSynchronize(s), "is_valid_fast");
+  if (stats) {
+    std::vector<unsigned long long> h((size_t)n_chunks * 8, 0);
+    cuda_check(cudaMemcpy(h.data(), ctl, (size_t)n_chunks * 64, cudaMemcpyDeviceToHost), "D2H");
+    stats[0] = B;
+    stats[1] = stats[2] = stats[3] = 0;
+    for (int64_t i = 0; i < n_chunks; i++) {
+      stats[1] += (int64_t)(unsigned)h[8 * i];
+      stats[2] += (int64_t)h[8 * i + 4];
+    }
+  }
+}
+
 int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats, int mem,
                             void* stream) {
   return guarded([&] {
@@ -1665,6 +1746,10 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
+    if (mem == PMGPU_MEM_HOST && B >= 16384) {
+      fast_host_pipelined(C, T, st, q, B, out, dist32, stats, s);
+      return;
+    }
     const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(4 * B, 1 << 16), (int64_t)1 << 28);
     int4* items = (int4*)C.f_items.ensure((size_t)cap * sizeof(int4));
     char* ctl = (char*)C.f_ctl.ensure(64);

@@ -289,3 +289,23 @@ def test_cloud_stats():
     assert st["list_entries"] > 0
     # at least the points (FP64 SoA + FP32) and the field (8 + 16 bytes per fine cell)
     assert st["device_bytes"] >= 40 * st["points"] + 24 * st["field_cells"]
+
+
+def test_fast_host_pipelined_matches_device(dual):
+    """A large host-memory batch runs in chunks on two streams (copies overlapping kernels); the
+    outcome equals the one-launch device-memory call: validity, distances and recheck counts."""
+    import torch
+
+    (_, cst, _), _ = dual
+    Q = W.dualarm_configs(20001, seed=23)  # ragged: the last chunk is short
+    ok_h, d_h, st_h = cst.is_valid_fast(Q, distances=True, stats=True)
+    ok_d, d_d, st_d = cst.is_valid_fast(torch.tensor(Q, device="cuda"), distances=True, stats=True)
+    assert np.array_equal(ok_h, ok_d.cpu().numpy())
+    assert np.array_equal(d_h, d_d.cpu().numpy())
+    assert st_h == st_d
+    # pinned host buffers, preallocated outputs
+    qp = torch.from_numpy(Q).pin_memory()
+    op = torch.empty(len(Q), dtype=torch.uint8).pin_memory()
+    dp = torch.empty((len(Q), cst.n_spheres), dtype=torch.float32).pin_memory()
+    cst.is_valid_fast(qp.numpy(), distances=True, out=op.numpy(), dist_out=dp.numpy())
+    assert np.array_equal(op.numpy(), ok_h) and np.array_equal(dp.numpy(), d_h)
