@@ -584,7 +584,7 @@ static std::vector<size_t> farthest_order(const std::vector<std::array<double, 3
 struct FastPipe {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  DevBuf in[2], out[2], dist[2], items[2];
+  DevBuf in[2], out[2], dist[2], items[2], hq[2];
   DevBuf ctl, ovf;  // per chunk counters (64 B each) and per-config overflow flags, for the whole call
   FastPipe() = default;
   FastPipe(const FastPipe&) = delete;
@@ -623,6 +623,7 @@ struct HostCst {
   // workspaces for host-memory calls
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
+  DevBuf f_hq;                        // fast-path hard cloud queries (distances mode)
   FastPipe pipe;                      // host-memory fast calls of large batches
   DevBuf e_sr, e_n, e_off;            // fast edge path: step ratios, waypoint counts and offsets
   DevBuf g_wp;                        // trajectory costs: per-waypoint partial costs
@@ -1681,6 +1682,13 @@ int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* t
     *threads_per_block = c->c.fast_nt;
   });
 }
+// Capacity of the global hard-query queue of a fast call with distances: 16 per configuration (the
+// dual-arm cloud batch needs about 8), at most one per sphere; a block whose queries do not fit
+// answers them itself.
+static unsigned hard_query_cap(int64_t B, int64_t ns) {
+  return (unsigned)std::min<int64_t>(std::min<int64_t>(B * ns, std::max<int64_t>(B * 16, 1 << 16)), (int64_t)1 << 26);
+}
+
 // Host-memory fast call of a large batch, in up to 8 chunks of at least 8,192 configurations on two
 // streams (FastPipe).  Every configuration is independent, so the outcome is the same as one launch.
 static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* st, const double* q, int64_t B, uint8_t* out,
@@ -1697,7 +1705,10 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
   uint8_t* dout[2];
   float* ddist[2];
   int4* items[2];
+  void* hqb[2];
+  const unsigned hq_cap = hard_query_cap(chunk, ns);
   for (int k = 0; k < 2; k++) {  // sized once per call, before any chunk is in flight
+    hqb[k] = dist32 ? P.hq[k].ensure((size_t)hq_cap * 32) : nullptr;
     din[k] = (double*)P.in[k].ensure((size_t)chunk * d * 8);
     dout[k] = (uint8_t*)P.out[k].ensure(std::max<size_t>((size_t)chunk, 16));
     ddist[k] = dist32 ? (float*)P.dist[k].ensure((size_t)chunk * ns * 4) : nullptr;
@@ -1716,7 +1727,7 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
     cuda_check(cudaMemcpyAsync(din[k], q + c0 * d, (size_t)(n * d) * 8, cudaMemcpyHostToDevice, cs), "H2D copy");
     char* cc = ctl + i * 64;
     cuda_check(launch_fast_valid(T, C.hdr, st, din[k], n, dout[k], ddist[k], 0.1f, items[k], (unsigned int*)cc, cap, ovf + c0,
-                                 (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs),
+                                 (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs, hqb[k], (unsigned long long*)(cc + 48), hq_cap),
                "is_valid_fast");
     cuda_check(cudaMemcpyAsync(out + c0, dout[k], (size_t)n, cudaMemcpyDeviceToHost, cs), "D2H copy");
     if (dist32) cuda_check(cudaMemcpyAsync(dist32 + c0 * ns, ddist[k], (size_t)(n * ns) * 4, cudaMemcpyDeviceToHost, cs), "D2H copy");
@@ -1766,7 +1777,10 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
       dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)B, 16));
       dd = dist32 ? (float*)C.w_out2.ensure(std::max<size_t>((size_t)B * C.n_spheres() * 4, 16)) : nullptr;
     }
-    cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s),
+    const unsigned hq_cap = hard_query_cap(B, C.n_spheres());
+    void* hq = dd ? C.f_hq.ensure((size_t)hq_cap * 32) : nullptr;
+    cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s, hq,
+                                 (unsigned long long*)(ctl + 48), hq_cap),
                "is_valid_fast");
     if (mem == PMGPU_MEM_HOST) {
       stage_out(out, dout, (size_t)B, s);

@@ -70,12 +70,23 @@ constexpr int kPoseF = 20;
 enum { ST_PASS = 0, ST_FAIL = 1, ST_MAYBE = 2 };
 constexpr int FLAG_FAIL = 1;
 
+// A hard cloud query handed from k_fast_valid to k_hard_queries (distances mode): the sphere centre
+// and search reach, then (configuration, sphere | primitive << 16 | validity check << 31, FK error
+// bound of the centre as float bits, 0).
+struct HardQuery {
+  float4 a;
+  int4 b;
+};
+
 struct Scratch {
   int4* items;
   unsigned int* count;
   unsigned int cap;
   uint8_t* overflow;
   unsigned long long* stats;
+  HardQuery* hq;           // global hard-query queue (distances mode), or null: queries stay in the block
+  unsigned long long* hq_count;  // entries reserved (64-bit: a large batch may reserve more than 2^32)
+  unsigned int hq_cap;
 };
 
 __device__ __forceinline__ float3 xf(const float* P, float x, float y, float z) {  // R (row-major 9) * v + t (P[9..11])
@@ -925,6 +936,35 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   {
     const int lane = tid & 31;
     const int nq = min(sm.hq_n[0], hq_cap);
+    if (want_dist && scr.hq != nullptr && nq > 0) {  // block-uniform
+      // with distances the queries go to k_hard_queries, which answers them without this block's
+      // barriers; what does not fit in the global queue is answered here below
+      if (tid == 0) {
+        const unsigned long long base = atomicAdd(scr.hq_count, (unsigned long long)nq);
+        const long long room = base >= scr.hq_cap ? 0 : (long long)scr.hq_cap - (long long)base;
+        sm.hq_n[2] = room > 0 ? (int)base : 0;  // base < hq_cap whenever an entry goes out
+        sm.hq_n[1] = room >= nq ? nq : (int)room;  // the local loop starts past these
+      }
+      __syncthreads();
+      const unsigned base = (unsigned)sm.hq_n[2];
+      const int n_out = sm.hq_n[1];
+      for (int k = tid; k < n_out; k += blockDim.x) {
+        const int2 e = sm.hq[k];
+        const int c = e.x >> 16, si = e.x & 0xffff;
+        const SphereF S = sm.sph[si];
+        const GroupF& G = sm.grp[S.group];
+        const PrimF& Pr = sm.prm[e.y];
+        const float* P = sm.pose + ((size_t)c * nsl + G.slot) * kPoseF;
+        const float3 sc = xf(P, S.x, S.y, S.z);
+        const float ek = P[12] + P[13] * S.sn;
+        const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
+        const float reach = Pr.a + S.r + (m + cutoff);
+        HardQuery h;
+        h.a = make_float4(sc.x, sc.y, sc.z, reach);
+        h.b = make_int4((int)(c0 + c), si | (e.y << 16) | (G.only_self ? 0 : (int)0x80000000u), __float_as_int(ek), 0);
+        scr.hq[base + k] = h;
+      }
+    }
     auto pop = [&]() {
       int k = 0;
       if (lane == 0) k = atomicAdd(&sm.hq_n[1], 1);
@@ -1176,6 +1216,73 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 64)) k_fast_edges(const PmTa
   }
 }
 
+// min(*a, v) for FP32 values of either sign: non-negative floats order like their int bits, negative
+// ones in reverse of their unsigned bits.
+__device__ __forceinline__ void atomic_min_float(float* a, float v) {
+  if (v >= 0.f)
+    atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+  else
+    atomicMax(reinterpret_cast<unsigned int*>(a), __float_as_uint(v));
+}
+
+// The hard cloud queries of a k_fast_valid launch with distances, one warp per query over the whole
+// queue (no per-block barrier), the next query's field records read before the current walk.  Same
+// arithmetic as the in-block answer: the distance goes into dist32 by an exact minimum, a certain
+// collision clears the configuration, an uncertain one goes to the recheck queue.
+template <class Src>
+__global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __restrict__ T, const HardQuery* __restrict__ hq,
+                                                         float* __restrict__ dist32, Src src, Scratch scr) {
+  TView v(T);
+  const int lane = threadIdx.x & 31;
+  const int ns = T->n_spheres;
+  const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  auto record = [&](int64_t i) {
+    if (i >= n) return make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    const HardQuery h = hq[i];
+    return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z);
+  };
+  float4 rec = record(k);
+  while (k < n) {  // warp-uniform
+    const int64_t kn = k + nw;
+    const float4 rec_n = record(kn);
+    const HardQuery h = hq[k];
+    const int cfg = h.b.x, si = h.b.y & 0xffff, prim = (h.b.y >> 16) & 0x7fff;
+    const bool check = h.b.y < 0;
+    const float ek = __int_as_float(h.b.z);
+    const float qx = h.a.x, qy = h.a.y, qz = h.a.z, reach = h.a.w;
+    const PmPrim& Pp = v.P[prim];
+    const float pa = (float)Pp.a, sr = (float)v.sr[si];
+    const NNResult32 start = field_corner_candidate(rec, qx, qy, qz);
+    const NNResult32 nn = warp_nearest32(v.C[Pp.cloud], qx, qy, qz, reach * reach, start.d2, start.idx);
+    if (lane == 0) {
+      float g, sd, mag;
+      if (nn.idx < 0) {
+        g = reach - pa - sr;
+        sd = 3.0e38f;
+        mag = fabsf(qx) + fabsf(qy) + fabsf(qz);
+      } else {
+        const float d = sqrtf(nn.d2);
+        g = d - pa - sr;
+        sd = g;
+        mag = fabsf(qx) + fabsf(qy) + fabsf(qz) + d;
+      }
+      atomic_min_float(dist32 + (int64_t)cfg * ns + si, sd);
+      if (check) {
+        const float mm = margin32(mag) + ek;
+        if (g < -mm) {
+          src.fail(cfg);
+        } else if (g <= mm) {
+          push_item(scr, src, cfg, prim << 1, si, nn.idx);
+        }
+      }
+    }
+    k = kn;
+    rec = rec_n;
+  }
+}
+
 // Exact FP64 evaluation of the queued terms, and full plain checks of the configurations (or
 // edges) whose terms overflowed the queue.
 template <class Src>
@@ -1359,9 +1466,12 @@ static cudaError_t prep(K kern, size_t sm) {
 // count, overflow and stats must be zeroed by the caller
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
-                              uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s) {
+                              uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq,
+                              unsigned long long* hq_count, unsigned int hq_cap) {
   if (B <= 0) return cudaSuccess;
-  Scratch scr{items, count, cap, overflow, stats};
+  const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0;
+  Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
+              split ? hq_cap : 0u};
   size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
@@ -1387,6 +1497,15 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_end("k_fast_valid", s);
   CfgSource src{q, B, out};
+  if (split) {
+    int dev = 0, n_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    prof_begin("k_hard_queries", s);
+    k_hard_queries<CfgSource><<<n_sm * 4, 256, 0, s>>>(T, scr.hq, dist32, src, scr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_end("k_hard_queries", s);
+  }
   prof_begin("k_fast_recheck", s);
   k_fast_recheck<CfgSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
   prof_end("k_fast_recheck", s);

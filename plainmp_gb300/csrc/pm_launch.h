@@ -39,9 +39,12 @@ cudaError_t launch_check_motion64(const PmTablesHdr* T, const double* state, con
 
 // ---- fast path (k_fast.cu): FP32 decisions + FP64 recheck of uncertain terms.
 size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist);
+// hq (hq_cap 32-byte entries) and hq_count (zeroed by the caller): with distances, the hard cloud
+// queries are answered by a second kernel over this global queue; null keeps them in the block.
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
-                              uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s);
+                              uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq = nullptr,
+                              unsigned long long* hq_count = nullptr, unsigned int hq_cap = 0);
 
 cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
                               int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,

@@ -302,7 +302,9 @@ def test_fast_host_pipelined_matches_device(dual):
     ok_d, d_d, st_d = cst.is_valid_fast(torch.tensor(Q, device="cuda"), distances=True, stats=True)
     assert np.array_equal(ok_h, ok_d.cpu().numpy())
     assert np.array_equal(d_h, d_d.cpu().numpy())
-    assert st_h == st_d
+    # the recheck statistics depend on warp timing (a self pair skips a configuration another warp
+    # has already found colliding), so only the outcome is compared, plus the configuration count
+    assert st_h["configs"] == st_d["configs"] == len(Q)
     # pinned host buffers, preallocated outputs
     qp = torch.from_numpy(Q).pin_memory()
     op = torch.empty(len(Q), dtype=torch.uint8).pin_memory()
