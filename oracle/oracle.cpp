@@ -1,7 +1,7 @@
 // Test infrastructure only -- NOT part of the product.
 //
-// CPU FP64 restatement of plainmp's collision-checking hot path, used as the parity
-// checker by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.  It is
+// CPU FP64 restatement of plainmp's collision-checking hot path, against which tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg compare the device path.  It is
 // written from the reference's behaviour (cited file:line per function, paths relative to
 // the plainmp project) and compiled with -ffp-contract=off; oracle/ORDER.md fixes the
 // arithmetic order.  Nothing in the product links or calls this file.

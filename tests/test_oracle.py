@@ -1,4 +1,4 @@
-"""CPU tests that pin the oracle (oracle/oracle.cpp) before it is trusted as the checker:
+"""CPU tests that pin the oracle (oracle/oracle.cpp) before the device path is compared with it:
 golden vectors produced by the reference itself (tests/golden/, see make_golden.py) and the
 reference's own known-answer and property tests restated (tests/test_psdf.py,
 tests/test_kdtree.py, tests/test_constraints.py of the plainmp project)."""
