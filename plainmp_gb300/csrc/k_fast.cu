@@ -308,7 +308,7 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   NNResult32 r{maxd2, -1};
-  if (G.n_points <= 0) return r;
+  if (G.n_points <= 0 || !isfinite(qx) || !isfinite(qy) || !isfinite(qz)) return r;  // as grid_nearest64
   // a known point (init_idx at init_d2, e.g. the nearest point of the query's field cell) starts the
   // walk with a tight bound
   float best = init_d2 < maxd2 ? init_d2 : maxd2;
@@ -324,7 +324,7 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
   for (int a = 0; a < 3; a++) {
     const float f = floorf((qa[a] - oa[a]) * inv);
     if (!(f >= 0.f && f <= (float)(nb[a] - 1))) inside = false;
-    cb[a] = f < 0.f ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
+    cb[a] = !(f >= 0.f) ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
   }
   auto process = [&](bool cand, int2 occ) {
     unsigned bal = __ballot_sync(FULL, cand);
@@ -463,7 +463,7 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
     for (int a = 0; a < 3; a++) {
       // 1e-3 block of slack covers the FP32 rounding of the range against the FP64 assignment
       const float f0 = floorf((qa[a] - reach - oa[a]) * inv - 1e-3f), f1 = floorf((qa[a] + reach - oa[a]) * inv + 1e-3f);
-      if (f1 < 0.f || f0 > (float)(nb[a] - 1)) return r;
+      if (!(f1 >= 0.f) || !(f0 <= (float)(nb[a] - 1))) return r;  // also rejects NaN
       lo[a] = f0 < 0.f ? 0 : (int)f0;
       hi[a] = f1 > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f1;
     }
@@ -765,7 +765,16 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       sm.flags[tid] = FLAG_FAIL | 2;  // already known invalid: no work
     } else {
       const double* qc = src.cfg(T, c0 + tid, qbuf + tid * T->q_dim);
-      fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, sm.pose + (size_t)tid * nsl * kPoseF);
+      bool finite = true;
+      for (int i = 0; i < T->q_dim; i++) finite = finite && isfinite(qc[i]);
+      if (finite) {
+        fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, sm.pose + (size_t)tid * nsl * kPoseF);
+      } else {
+        // a NaN or infinite coordinate makes every FP32 bound NaN, and no decision would be taken:
+        // the exact FP64 check of the recheck kernel decides, as for an overflowing queue
+        sm.flags[tid] = 2;
+        scr.overflow[src.overflow_slot(c0 + tid)] = 1;
+      }
     }
   }
   __syncthreads();
@@ -1036,7 +1045,11 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   }
   __syncthreads();
   if (want_dist)
-    for (int t = tid; t < ncfg * ns; t += blockDim.x) dist32[c0 * ns + t] = o2f(sm.sdist[t]);  // sdist is [cfg][sphere]
+    for (int t = tid; t < ncfg * ns; t += blockDim.x) {  // sdist is [cfg][sphere]
+      const int c = t / ns;
+      // a configuration left to the exact check (non-finite coordinates) has no FP32 distances
+      dist32[c0 * ns + t] = (sm.flags[c] & 2) && !(sm.flags[c] & FLAG_FAIL) ? __int_as_float(0x7fc00000) : o2f(sm.sdist[t]);
+    }
   __syncthreads();
   if (tid < ncfg && !(sm.flags[tid] & 2)) src.done(c0 + tid, (sm.flags[tid] & FLAG_FAIL) != 0);
   __syncthreads();

@@ -43,7 +43,9 @@ struct NNResult64 {
 // (rings inside it hold no point) and is bounded by the grid size.
 __device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q, double maxd2 = INFINITY) {
   NNResult64 r{maxd2, -1};
-  if (G.n_points <= 0) return r;
+  // a NaN or infinite query is farther than every bound from every point (the KD-tree's
+  // comparisons all fail the same way); it must not reach the block arithmetic below
+  if (G.n_points <= 0 || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z)) return r;
   const double inv = 1.0 / G.block;
   int cb[3];
   const double qa[3] = {q.x, q.y, q.z};
@@ -52,7 +54,7 @@ __device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q, dou
   for (int a = 0; a < 3; a++) {
     double f = floor((qa[a] - G.origin[a]) * inv);
     if (!(f >= 0 && f <= nb[a] - 1)) inside = false;
-    int c = f < 0 ? 0 : (f > nb[a] - 1 ? nb[a] - 1 : (int)f);
+    int c = !(f >= 0) ? 0 : (f > nb[a] - 1 ? nb[a] - 1 : (int)f);
     cb[a] = c;
   }
   const int k0 = G.edf[cb[0] + nb[0] * (cb[1] + nb[1] * cb[2])];
@@ -128,7 +130,7 @@ __device__ __forceinline__ float box_d2_32(const float* b, float qx, float qy, f
 // when none is closer).
 __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2 = INFINITY) {
   NNResult32 r{maxd2, -1};
-  if (G.n_points <= 0) return r;
+  if (G.n_points <= 0 || !isfinite(qx) || !isfinite(qy) || !isfinite(qz)) return r;  // as grid_nearest64
   const float inv = G.inv_blk32;
   const float ox = G.o32[0], oy = G.o32[1], oz = G.o32[2];
   const float blk = G.blk32;
@@ -140,7 +142,7 @@ __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float 
   for (int a = 0; a < 3; a++) {
     float f = floorf((qa[a] - oa[a]) * inv);
     if (!(f >= 0.f && f <= (float)(nb[a] - 1))) inside = false;
-    cb[a] = f < 0.f ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
+    cb[a] = !(f >= 0.f) ? 0 : (f > (float)(nb[a] - 1) ? nb[a] - 1 : (int)f);
   }
   if (inside && G.blk_list) {  // the block's candidate list covers every point within its reach
     const int b = cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]);

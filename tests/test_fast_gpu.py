@@ -311,3 +311,24 @@ def test_fast_host_pipelined_matches_device(dual):
     dp = torch.empty((len(Q), cst.n_spheres), dtype=torch.float32).pin_memory()
     cst.is_valid_fast(qp.numpy(), distances=True, out=op.numpy(), dist_out=dp.numpy())
     assert np.array_equal(op.numpy(), ok_h) and np.array_equal(dp.numpy(), d_h)
+
+
+def test_fast_non_finite_configurations(chain, dual):
+    """Configurations with a NaN or infinite coordinate get the exact FP64 decision (their FP32
+    bounds would be NaN and decide nothing): validity equals the plain method and the oracle,
+    and their FP32 distances are NaN; every other row is unaffected."""
+    for (_, cst, _), (_, oc, _), Q in ((chain[0], chain[1], W.chain7_configs(300, seed=41)),
+                                       (dual[0], dual[1], W.dualarm_configs(300, seed=42))):
+        Q = Q.copy()
+        bad = np.zeros(len(Q), dtype=bool)
+        for i, v in ((3, np.nan), (17, np.inf), (18, -np.inf), (150, np.nan), (299, np.nan)):
+            Q[i, i % Q.shape[1]] = v
+            bad[i] = True
+        plain = np.asarray(cst.is_valid_batch(Q))
+        assert np.array_equal(plain, oc.is_valid(Q))
+        assert np.array_equal(cst.is_valid_fast(Q), plain)
+        ok, d = cst.is_valid_fast(Q, distances=True)
+        assert np.array_equal(ok, plain)
+        assert np.isnan(d[bad]).all()
+        ok_clean, d_clean = cst.is_valid_fast(Q[~bad], distances=True)
+        assert np.array_equal(d[~bad], d_clean) and np.array_equal(ok[~bad], ok_clean)
