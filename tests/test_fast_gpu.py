@@ -332,3 +332,21 @@ def test_fast_non_finite_configurations(chain, dual):
         assert np.isnan(d[bad]).all()
         ok_clean, d_clean = cst.is_valid_fast(Q[~bad], distances=True)
         assert np.array_equal(d[~bad], d_clean) and np.array_equal(ok[~bad], ok_clean)
+
+
+def test_fast_degenerate_clouds(oracle):
+    """An empty cloud, a single point and 50 coincident points (ties everywhere): validity equals
+    the oracle on both paths, and the FP32 distances match the plain FP64 ones (clamped)."""
+    robot = W.dualarm_robot()
+    Q = W.dualarm_configs(200, seed=44)
+    for pts in (np.zeros((0, 3)), np.array([[0.3, 0.0, 0.9]]), np.repeat([[0.4, 0.1, 0.8]], 50, axis=0)):
+        scene = W.Scene(cloud=pts.astype(np.float32), cloud_radius=0.01)
+        _, cst, _ = scenes.make_constraint(robot, scene)
+        _, oc, _ = oracle.make_constraint(robot, scene)
+        ref = oc.is_valid(Q, threads=8)
+        assert np.array_equal(cst.is_valid_batch(Q), ref), len(pts)
+        assert np.array_equal(cst.is_valid_fast(Q), ref), len(pts)
+        ok, d = cst.is_valid_fast(Q, distances=True)
+        assert np.array_equal(ok, ref), len(pts)
+        d_ref = np.minimum(cst.sphere_distances(Q), CUTOFF)
+        assert np.abs(d.astype(np.float64) - d_ref).max() < DIST_TOL, len(pts)
