@@ -545,6 +545,12 @@ def main():
     ok_plain = cst.is_valid_batch(Q).cpu().numpy()
     mismatches = int((ok_fast != ok_plain).sum())
     _, st = cst.is_valid_fast(Q, stats=True)
+    # FP32 distance error on a sample: the fast path's per-sphere distances against the plain FP64
+    # method's (both clamped at the 0.1 m cutoff)
+    n_err = min(B, 4096)
+    _, d32 = cst.is_valid_fast(Q[:n_err], distances=True)
+    d64 = torch.clamp(torch.as_tensor(cst.sphere_distances(Q[:n_err])), max=0.1)
+    dist_err = float((d32.double() - d64).abs().max())
 
     # end to end through the public API with pinned host buffers (copies inside the region)
     qpin = torch.from_numpy(qh).pin_memory()
@@ -620,7 +626,10 @@ def main():
         "fast_validity_only": {"value": B / (ms_valid / 1e3), "unit": "configs/s", "ms_per_batch": ms_valid},
         "speedup_vs_plain": {"with_distances": ms_plain / ms_per_step, "validity_only": ms_plain / ms_valid},
         "validity_mismatches_fast_vs_plain": mismatches,
-        "recheck": {"terms": st["rechecked_terms"], "configs_full": st["rechecked_configs"], "recheck_kernel_ms": r_ms / max(r_n, 1)},
+        "recheck": {"terms": st["rechecked_terms"], "terms_per_config": st["rechecked_terms"] / B,
+                    "configs_full": st["rechecked_configs"], "recheck_kernel_ms": r_ms / max(r_n, 1)},
+        "distance_error": {"sample_configs": n_err, "max_abs_m": dist_err,
+                           "vs": "plain FP64 per-sphere distances, both clamped at 0.1 m"},
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
