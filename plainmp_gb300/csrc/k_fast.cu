@@ -653,10 +653,14 @@ __device__ __forceinline__ int f2o(float f) {
 __device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
 template <class Src>
-__device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int b, int kind_x, int i, int j) {
+__device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int64_t b, int kind_x, int i, int j) {
+  if (b > 0x7fffffffLL) {  // the queue stores 32-bit indices: beyond them, the full FP64 check decides
+    s.overflow[src.overflow_slot(b)] = 1;
+    return;
+  }
   unsigned int k = atomicAdd(s.count, 1u);
   if (k < s.cap) {
-    s.items[k] = make_int4(b, kind_x, i, j);
+    s.items[k] = make_int4((int)b, kind_x, i, j);
   } else {
     s.overflow[src.overflow_slot(b)] = 1;
   }
@@ -870,7 +874,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         fail = 1;
         if (!want_dist) break;
       } else if (g <= mm) {
-        push_item(scr, src, (int)(c0 + c), p << 1, si, -1);
+        push_item(scr, src, c0 + c, p << 1, si, -1);
       }
     }
     if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
@@ -931,7 +935,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
             const float mm = 2.0f * margin32(fabsf(ci.x) + fabsf(ci.y) + fabsf(ci.z) + fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z)) +
                              P1[12] + P1[13] * Si.sn + P2[12] + P2[13] * Sj.sn;
             if (g < -mm) fail = 1;
-            else if (g <= mm) push_item(scr, src, (int)(c0 + c), (pi << 1) | 1, G1.begin + i, G2.begin + j);
+            else if (g <= mm) push_item(scr, src, c0 + c, (pi << 1) | 1, G1.begin + i, G2.begin + j);
           }
         }
         if (__any_sync(FULL, fail)) break;
@@ -1034,7 +1038,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
             if (g < -mm) {
               atomicOr(&sm.flags[c], FLAG_FAIL);
             } else if (g <= mm) {
-              push_item(scr, src, (int)(c0 + c), e.y << 1, si, nn.idx);
+              push_item(scr, src, c0 + c, e.y << 1, si, nn.idx);
             }
           }
         }
@@ -1482,7 +1486,8 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq,
                               unsigned long long* hq_count, unsigned int hq_cap) {
   if (B <= 0) return cudaSuccess;
-  const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0;
+  // (hard-query entries hold 32-bit configuration indices)
+  const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
               split ? hq_cap : 0u};
   size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
