@@ -249,3 +249,25 @@ def test_sequential_cst_bookkeeping():
     s.finalize()
     assert s.cst_dim() == 9 + 14 + 56
     assert "fixed point: 7" in str(s)
+
+
+def test_bench_reference_arm_line():
+    """bench.py --impl reference (the CPU restatement on the host cores) prints the one JSON line
+    of the benchmark contract, with the reference arm's own cpu_baseline and a zero-copy e2e."""
+    import json
+    import subprocess
+    import sys
+
+    r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "1"],
+                       capture_output=True, text=True, timeout=300, cwd=str(REPO))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["metric"] == "configs checked/sec" and d["unit"] == "configs/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
