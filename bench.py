@@ -192,6 +192,10 @@ def bench_chain7(dev, timed):
     ms_fast = timed(lambda: cst.is_valid_fast(Q, distances=True), 10)
     same = bool(torch.equal(cst.is_valid_fast(Q), cst.is_valid_batch(Q)))
     s1, s2 = W.chain7_edges(1024)
+    # waypoints checked per edge without early exit (box validator, width 0.05): floor(max|dq| / w) + 1
+    wp = np.floor(np.abs(s2 - s1).max(axis=1) / 0.05).astype(np.int64) + 1
+    wp_hist = {"min": int(wp.min()), "max": int(wp.max()), "mean": float(wp.mean()), "total": int(wp.sum()),
+               "deciles": [int(x) for x in np.percentile(wp, np.arange(10, 100, 10))]}
     S1, S2 = torch.tensor(s1, device=dev), torch.tensor(s2, device=dev)
     mv = BoxMotionValidator(cst, [0.05] * 7)
     ms_e_plain = timed(lambda: mv.check_motion_batch(S1, S2), 5)
@@ -212,7 +216,7 @@ def bench_chain7(dev, timed):
                "unit": "edges/s", "plain_fp64": 1024 / (ms_e_plain / 1e3), "fast_persistent": 1024 / (ms_e_fast / 1e3),
                "fast_cuda_graph": 1024 / (ms_e_graph / 1e3) if ms_e_graph else None,
                "ms": {"plain_fp64": ms_e_plain, "fast_persistent": ms_e_fast, "fast_cuda_graph": ms_e_graph},
-               "edge_validity_identical": same_e},
+               "edge_validity_identical": same_e, "waypoints_per_edge": wp_hist},
     }
 
 
