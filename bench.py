@@ -146,6 +146,7 @@ def cpu_baseline(robot, scene, q, seconds: float = 6.0):
             "sample": f"{done} configs of the same batch ({reps} x {n}), validity only (the reference has no per-sphere distance output)"}
 
 
+C0_FLOP = 7 * 90 + 8 * 24 + 56 * 18 + 56 * (35 * 10 + 11 * 5 + 30 * 5) + 960 * 11  # per configuration, the counting rule
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
 
 
@@ -211,7 +212,14 @@ def bench_chain7(dev, timed):
         "C0": {"workload": "7-joint chain, 56 spheres, 10 boxes + 5 spheres + 5 cylinders, 4096 configurations",
                "unit": "configs/s", "plain_fp64": 4096 / (ms_plain / 1e3), "fast_with_distances": 4096 / (ms_fast / 1e3),
                "ms": {"plain_fp64": ms_plain, "fast_with_distances": ms_fast}, "validity_identical": same,
-               "launch_shape": list(shape0)},
+               "launch_shape": list(shape0),
+               # algorithmic work per configuration with no early exit and no broad phase: FK 7 x 90,
+               # rotations 8 x 24, sphere transforms 56 x 18, narrow phase 56 x (35 x 10 + 11 x 5 + 30 x 5),
+               # self pairs 960 x 11; the kernels skip most of it (culling, early exit), so these
+               # "effective" rates exceed the arithmetic peaks by design
+               "effective": {"kflop_per_config": C0_FLOP / 1e3,
+                             "fast_tflops": 4096 / (ms_fast / 1e3) * C0_FLOP / 1e12,
+                             "plain_tflops": 4096 / (ms_plain / 1e3) * C0_FLOP / 1e12}},
         "C1": {"workload": "1024 straight edges on the C0 chain and scene, box validator width 0.05 rad, 1-120 waypoints",
                "unit": "edges/s", "plain_fp64": 1024 / (ms_e_plain / 1e3), "fast_persistent": 1024 / (ms_e_fast / 1e3),
                "fast_cuda_graph": 1024 / (ms_e_graph / 1e3) if ms_e_graph else None,
