@@ -1,17 +1,21 @@
 // FP32 fast path with FP64 recheck (validity booleans identical to the plain method).
 //
-// Per block of CPB configurations:
+// Per block of CPB configurations (k_fast_valid; k_fast_edges over the waypoints of edges):
 //   1. FK in FP32 into shared memory, with a running bound on each slot's error against the
 //      FP64 FK of the reference (see fk32); every later margin adds the bound of the spheres
-//      involved;
+//      involved.  A configuration with a non-finite coordinate goes to the exact FP64 check;
 //   2. group culling: the clearance of each sphere group's bounding sphere against each
-//      primitive (a point cloud: a radius-bounded FP32 nearest-neighbour query);
-//   3. sphere tasks (sphere x primitive) and self-pair tasks (group pair x sphere pairs), each
-//      decision a tri-state of an FP32 clearance g against a margin m derived from the FP32
-//      error bound: pass if g > m, fail if g < -m, otherwise the term is queued;
+//      primitive (a point cloud: the lower bound of its nearest-point field);
+//   3. sphere tasks (sphere x primitive) and self-pair tasks (a group test per lane, then the
+//      surviving group pairs by the whole warp), each decision a tri-state of an FP32 clearance g
+//      against a margin m derived from the FP32 error bound: pass if g > m, fail if g < -m,
+//      otherwise the term is queued.  Spheres near a point cloud need its exact nearest point:
+//      a warp-cooperative search over the block's candidate list, in the block, or with
+//      distances in k_hard_queries over a global queue;
 //   4. k_fast_recheck evaluates every queued term with the exact FP64 gate-and-test of the
 //      reference (primitive_sphere_collision.cpp:191-254) and clears the configuration if the
-//      term collides.
+//      term collides; configurations (edges) whose terms did not fit the queue get the full
+//      FP64 check.
 // Why the terms suffice: ext collision = OR over groups g and primitives p of
 // [gate(g,p) AND OR_s test(s,p)] = OR over (s,p) of [gate(g(s),p) AND test(s,p)]; a sphere
 // that certainly collides by more than the margin lies inside its group sphere, whose gate then
