@@ -212,6 +212,31 @@ class Batch:
             self.stream = C.c_void_p(0)
             self.shape = self.keep.shape
 
+    def out(self, buf, shape, dtype):
+        """Pointer to a caller's preallocated output, which the call writes in place: it must be
+        a C-contiguous, writeable array of exactly this shape and dtype in this batch's memory
+        space (a CUDA tensor on the same device, or a host array).  Anything else raises
+        ValueError: a converted copy would receive the results instead, and a smaller buffer
+        would be overrun."""
+        shape = tuple(int(x) for x in shape)
+        if self.mem == MEM_DEVICE:
+            tdt = {np.float64: self.torch.float64, np.float32: self.torch.float32, np.uint8: self.torch.uint8,
+                   np.int64: self.torch.int64}[dtype]
+            ok = (isinstance(buf, self.torch.Tensor) and buf.is_cuda and buf.device == self.keep.device and buf.dtype == tdt
+                  and buf.is_contiguous() and tuple(buf.shape) == shape)
+            if not ok:
+                raise ValueError(f"output buffer must be a contiguous {tdt} CUDA tensor of shape {shape} on {self.keep.device}")
+            return C.c_void_p(buf.data_ptr())
+        if type(buf).__module__.startswith("torch"):  # a torch tensor, whatever the input was
+            if buf.is_cuda:
+                raise ValueError("output buffer must be in host memory, like the input")
+            buf = buf.detach().numpy()  # shares the tensor's memory
+        ok = (isinstance(buf, np.ndarray) and buf.dtype == np.dtype(dtype) and buf.flags.c_contiguous and buf.flags.writeable
+              and buf.shape == shape)
+        if not ok:
+            raise ValueError(f"output buffer must be a C-contiguous, writeable {np.dtype(dtype)} host array of shape {shape}")
+        return C.c_void_p(buf.ctypes.data)
+
     def empty(self, shape, dtype):
         """An output buffer in the same memory space."""
         if self.mem == MEM_DEVICE:

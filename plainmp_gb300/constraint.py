@@ -190,11 +190,11 @@ class SphereCollisionCst:
         arrays) in the same memory space as Q."""
         b = self._batch(Q)
         if out is not None:
-            optr = Batch(out, np.uint8).ptr
+            optr = b.out(out, (b.shape[0],), np.uint8)
         else:
             out, optr = b.empty((b.shape[0],), np.uint8)
         if distances and dist_out is not None:
-            dist, dp = dist_out, Batch(dist_out, np.float32).ptr
+            dist, dp = dist_out, b.out(dist_out, (b.shape[0], self.n_spheres), np.float32)
         else:
             dist, dp = b.empty((b.shape[0], self.n_spheres), np.float32) if distances else (None, None)
         st = np.zeros(4, dtype=np.int64)

@@ -61,7 +61,7 @@ class _ValidatorBase:
         b1, b2 = self._edges(S1, S2)
         E = b1.shape[0]
         if out is not None:
-            optr = Batch(out, np.uint8).ptr
+            optr = b1.out(out, (b1.shape[0],), np.uint8)
         else:
             out, optr = b1.empty((E,), np.uint8)
         w = self._width_arg(b1)

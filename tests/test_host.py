@@ -271,3 +271,29 @@ def test_bench_reference_arm_line():
     assert d["value"] > 0 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_output_buffers_are_validated():
+    """A preallocated output is written in place, so one of the wrong dtype, shape or layout is
+    refused before any device work (a converted copy would receive the results instead, and a
+    short buffer would be overrun)."""
+    from plainmp_gb300 import BoxMotionValidator, scenes
+    from plainmp_gb300 import workloads as W
+
+    _, cst, _ = scenes.make_constraint(W.chain7_robot(), W.chain7_scene())
+    Q = W.chain7_configs(8)
+    ns = cst.n_spheres
+    for bad in (np.zeros(8, np.int32), np.zeros(7, np.uint8), np.zeros(16, np.uint8)[::2], np.zeros((8, 1), np.uint8)):
+        with pytest.raises(ValueError):
+            cst.is_valid_fast(Q, out=bad)
+    for bad in (np.zeros((8, ns), np.float64), np.zeros((8, ns + 1), np.float32), np.zeros((ns, 8), np.float32).T):
+        with pytest.raises(ValueError):
+            cst.is_valid_fast(Q, distances=True, out=np.zeros(8, np.uint8), dist_out=bad)
+    ro = np.zeros(8, np.uint8)
+    ro.setflags(write=False)
+    with pytest.raises(ValueError):
+        cst.is_valid_fast(Q, out=ro)
+    s1, s2 = W.chain7_edges(4)
+    mv = BoxMotionValidator(cst, [0.05] * 7)
+    with pytest.raises(ValueError):
+        mv.check_motion_fast(s1, s2, out=np.zeros(3, np.uint8))
