@@ -691,7 +691,6 @@ struct CfgSource {  // a batch of configurations q[B x q_dim]
   const double* q;
   int64_t B;
   uint8_t* out;
-  __device__ int64_t count() const { return B; }
   __device__ const double* cfg(const PmTablesHdr* T, int64_t i, double*) const { return q + i * T->q_dim; }
   __device__ bool pre_skip(int64_t) const { return false; }     // before the fast pass: nothing known
   __device__ bool skip(int64_t i) const { return out[i] == 0; }  // after it: already invalid

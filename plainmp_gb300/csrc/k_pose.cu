@@ -110,7 +110,6 @@ __device__ void link_jacobian(const TView& v, const DPose* pose, int es, int rot
 struct Poses {
   DPose p[PM_MAX_SLOTS];
   __device__ DPose& operator[](int k) { return p[k]; }
-  __device__ const DPose& operator[](int k) const { return p[k]; }
 };
 
 // evaluate(q) of the constraint = update_kintree(q, high accuracy) + evaluate_dirty: vals
