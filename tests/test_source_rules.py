@@ -1,0 +1,66 @@
+"""Source rules of the CUDA kernels, checked on the text (no GPU, no compiler).
+
+A warp intrinsic with a full member mask (`__shfl_sync(0xffffffff, ...)`, `__any_sync`,
+`__ballot_sync`, ...) must be executed by every non-exited lane the mask names, at the same call.
+If some lanes skip it, the behaviour is undefined. The warp's lanes can then pair up at different
+sync points, and later shuffles return values from lanes that run other code.
+
+The usual way to break this is a conditionally evaluated call: `have && __shfl_sync(...)` or
+`c ? __shfl_sync(...) : x`, or an unbraced `if (c) v = __shfl_sync(...)`. A lane whose condition is
+false skips the call. The rule below rejects a warp intrinsic that is preceded in its own
+statement by `&&`, `||`, `?` or an `if (...)` header. Loops and braced branches whose condition is
+warp-uniform are left to review.
+"""
+import re
+from pathlib import Path
+
+import pytest
+
+CSRC = Path(__file__).resolve().parent.parent / "plainmp_gb300" / "csrc"
+
+_INTRINSIC = re.compile(
+    r"__(?:shfl|shfl_up|shfl_down|shfl_xor|any|all|ballot|match_any|match_all|reduce_[a-z]+|syncwarp)(?:_sync)?\s*\("
+)
+
+
+def _strip_comments(src: str) -> str:
+    src = re.sub(r"/\*.*?\*/", lambda m: "\n" * m.group(0).count("\n"), src, flags=re.S)
+    return re.sub(r"//[^\n]*", "", src)
+
+
+def conditional_warp_calls(src: str):
+    """(line, statement prefix) of every warp intrinsic that its own statement evaluates conditionally."""
+    s = _strip_comments(src)
+    found = []
+    for m in _INTRINSIC.finditer(s):
+        i = m.start()
+        start = max(s.rfind(";", 0, i), s.rfind("{", 0, i), s.rfind("}", 0, i))
+        prefix = s[start + 1 : i]
+        # a `for (init; cond; step)` header splits at its semicolons; the prefix is then the rest
+        # of the header, which is unconditional when the intrinsic sits in the loop condition
+        cond = re.search(r"&&|\|\||\?", prefix) or re.match(r"\s*(?:else\s+)?if\s*\(.*\)\s*\S", prefix, flags=re.S)
+        if cond:
+            found.append((s.count("\n", 0, i) + 1, " ".join(prefix.split())[-80:]))
+    return found
+
+
+def test_rule_catches_conditional_calls():
+    planted = """
+    __device__ void f(bool have, int v) {
+      const bool want = have && __shfl_sync(0xffffffffu, v, 0, 16) != 0;   // skipped where !have
+      int w = have ? __shfl_sync(0xffffffffu, v, 0) : 0;
+      if (have) v = __shfl_xor_sync(0xffffffffu, v, 1);
+      const int ok = __shfl_sync(0xffffffffu, have ? 1 : 0, 0);             // fine: the argument only
+      while (__any_sync(0xffffffffu, v > 0)) { v--; }                      // fine
+    }
+    """
+    lines = [ln for ln, _ in conditional_warp_calls(planted)]
+    assert lines == [3, 4, 5], lines
+
+
+@pytest.mark.parametrize("path", sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")), ids=lambda p: p.name)
+def test_warp_intrinsics_are_unconditional(path):
+    bad = conditional_warp_calls(path.read_text())
+    assert not bad, f"{path.name}: warp intrinsic evaluated conditionally at " + "; ".join(
+        f"line {ln}: ...{ctx}" for ln, ctx in bad
+    )
