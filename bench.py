@@ -116,6 +116,18 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def issue_rate(warp_inst, kernel_ms, sm_mhz, n_sm):
+    """Issue utilisation of an issue-bound kernel: warp instructions per launch (ncu
+    smsp__inst_executed.sum) over the launch's CUDA-event duration, against the SM's ceiling of 4
+    schedulers x 1 warp instruction per cycle at the SM clock sampled during the timed region.
+    None when a figure is missing."""
+    if not warp_inst or not kernel_ms or not sm_mhz or not n_sm:
+        return None
+    achieved = warp_inst / (kernel_ms / 1e3) / 1e9
+    peak = 4.0 * n_sm * sm_mhz / 1e3
+    return {"achieved": achieved, "peak": peak, "unit": "G warp instructions/s", "frac": achieved / peak}
+
+
 def peaks():
     if PEAKS.exists():
         d = json.loads(PEAKS.read_text())
@@ -589,10 +601,20 @@ def main():
     alg_bytes = B * (cst.q_dim() * 8 + 1 + ns * 4)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     prof = ROOT / "profiles" / "k_fast_valid_dualarm65536.traffic.json"
-    traffic, issue = None, None
+    traffic, issue, inst = None, None, {}
     if prof.exists():
         pj = json.loads(prof.read_text())
         traffic, issue = pj.get("dram_bytes_per_launch"), pj.get("issue_active_pct")
+        inst = {k: v.get("warp_instructions") for k, v in pj.get("per_kernel", {}).items()}
+    clocks = clk.summary()
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    k_each = {"k_fast_valid": k_ms / max(k_n, 1), "k_hard_queries": h_ms / max(h_n, 1)}
+    issue_each = {k: issue_rate(inst.get(k), k_each[k], clocks["sm_mhz"], n_sm) for k in k_each}
+    issue_step = issue_rate(sum(v or 0 for v in inst.values()), kernel_ms, clocks["sm_mhz"], n_sm)
+    if issue_step is not None:
+        issue_step.update({"per_kernel": issue_each,
+                           "instructions": "ncu smsp__inst_executed.sum of one launch of each kernel at launch shape (32, 512), "
+                                           "profiles/k_fast_valid_dualarm65536.traffic.json"})
 
     side = None
     fma_peaks = None
@@ -631,8 +653,9 @@ def main():
                      "kernel_ms_each": {"k_fast_valid": k_ms / max(k_n, 1), "k_hard_queries": h_ms / max(h_n, 1),
                                         "k_fast_recheck": r_ms / max(r_n, 1)},
                      "note": "HBM is not the binding resource: the kernel is issue/latency bound"
-                             + (f" (ncu: SM issue active {issue} %, profiles/k_fast_valid_dualarm65536.md)" if issue else "")},
-        "clocks": clk.summary(),
+                             + (f" (ncu: SM issue active {issue} %, profiles/k_fast_valid_dualarm65536.md)" if issue else ""),
+                     "issue": issue_step},
+        "clocks": clocks,
         "plain_fp64": {"value": B / (ms_plain / 1e3), "unit": "configs/s", "ms_per_batch": ms_plain,
                        "what": "plain FP64 method, one thread per configuration, validity only"},
         "fast_validity_only": {"value": B / (ms_valid / 1e3), "unit": "configs/s", "ms_per_batch": ms_valid},

@@ -297,3 +297,24 @@ def test_output_buffers_are_validated():
     mv = BoxMotionValidator(cst, [0.05] * 7)
     with pytest.raises(ValueError):
         mv.check_motion_fast(s1, s2, out=np.zeros(3, np.uint8))
+
+
+def test_bench_issue_rate():
+    """The issue-utilisation figure of the bench line: the committed capture's warp instructions per
+    launch over a launch time, against 4 warp instructions per SM per cycle."""
+    import json
+    import sys
+
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    assert bench.issue_rate(None, 1.0, 2070.0, 152) is None
+    assert bench.issue_rate(1e9, 1.0, None, 152) is None
+    r = bench.issue_rate(1258.56e6, 1.0, 2070.0, 152)  # exactly the ceiling for 1 ms at 2070 MHz
+    assert abs(r["frac"] - 1.0) < 1e-12 and abs(r["peak"] - 1258.56) < 1e-9
+    pj = json.loads((REPO / "profiles" / "k_fast_valid_dualarm65536.traffic.json").read_text())
+    per = pj["per_kernel"]
+    assert pj["warp_instructions_per_launch"] == sum(v["warp_instructions"] for v in per.values())
+    for k, v in per.items():  # the capture's own durations give its issue-active share, roughly
+        f = bench.issue_rate(v["warp_instructions"], v["ms"], 2070.0, 152)["frac"]
+        assert abs(f * 100 - v["issue_active_pct"]) < 6.0, (k, f)
