@@ -980,6 +980,8 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         h.b = make_int4((int)(c0 + c), si | (e.y << 16) | (G.only_self ? 0 : (int)0x80000000u), __float_as_int(ek), 0);
         scr.hq[base + k] = h;
       }
+      // the pops below advance hq_n[1]: every thread reads n_out (above) before any warp pops
+      __syncthreads();
     }
     auto pop = [&]() {
       int k = 0;
