@@ -886,6 +886,11 @@ void check_mem(int mem) {
 void check_ptr(const void* p, const char* what) {
   if (!p) throw std::invalid_argument(std::string(what) + " is NULL");
 }
+// A required array of a batch call: NULL is refused unless the batch is empty (in device memory a
+// NULL array would fault the kernel that reads it; in host memory, the copy).
+void check_arr(const void* p, int64_t n, const char* what) {
+  if (n > 0 && !p) throw std::invalid_argument(std::string(what) + " is NULL");
+}
 
 // Device image of an SDF tree for SDF-level calls
 const PmPrim* sdf_image(pmgpu_sdf* h, int* n_prims, const PmGridDev** clouds) {
@@ -1371,6 +1376,8 @@ int pmgpu_sdf_evaluate(pmgpu_sdf* s, const double* points, int64_t n, double* ou
     check_ptr(s, "sdf");
     check_mem(mem);
     if (n < 0) throw std::invalid_argument("negative count");
+    check_arr(points, n, "points");
+    check_arr(out, n, "out");
     int np;
     const PmGridDev* cl;
     const PmPrim* pr = sdf_image(s, &np, &cl);
@@ -1392,6 +1399,9 @@ int pmgpu_sdf_is_outside(pmgpu_sdf* s, const double* points, const double* radii
     check_ptr(s, "sdf");
     check_mem(mem);
     if (n < 0) throw std::invalid_argument("negative count");
+    check_arr(points, n, "points");
+    check_arr(radii, n, "radii");
+    check_arr(out, n, "out");
     int np;
     const PmGridDev* cl;
     const PmPrim* pr = sdf_image(s, &np, &cl);
@@ -1414,6 +1424,8 @@ int pmgpu_cloud_nearest(pmgpu_sdf* cloud, const double* points, int64_t n, doubl
     check_ptr(cloud, "cloud");
     check_mem(mem);
     if (cloud->s->kind != PM_SDF_CLOUD) throw std::invalid_argument("not a CloudSDF");
+    if (n < 0) throw std::invalid_argument("negative count");
+    check_arr(points, n, "points");
     int np;
     const PmGridDev* cl;
     sdf_image(cloud, &np, &cl);
@@ -1582,6 +1594,8 @@ int pmgpu_cst_is_valid(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, i
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
+    check_arr(out, B, "out");
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
@@ -1602,6 +1616,9 @@ int pmgpu_cst_evaluate(pmgpu_cst* c, const double* q, int64_t B, double* vals, d
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
+    check_arr(vals, B * C.cst_dim(), "vals");
+    check_arr(jac, B * C.cst_dim() * C.q_dim(), "jac");
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
@@ -1624,7 +1641,9 @@ int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int hig
   return guarded([&] {
     check_ptr(c, "cst");
     check_mem(mem);
+    if (B < 0) throw std::invalid_argument("negative batch");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
@@ -1754,6 +1773,8 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
+    check_arr(out, B, "out");
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
@@ -1806,7 +1827,11 @@ int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t
     check_mem(mem);
     if (validator_type != PMGPU_VALIDATOR_BOX && validator_type != PMGPU_VALIDATOR_EUCLIDEAN)
       fail(PMGPU_ERR_RUNTIME, "unknown validator type");
+    if (E < 0) throw std::invalid_argument("negative edge count");
     HostCst& C = c->c;
+    check_arr(s1, E * C.q_dim(), "s1");
+    check_arr(s2, E * C.q_dim(), "s2");
+    check_arr(out, E, "out");
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
@@ -1854,6 +1879,9 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
       fail(PMGPU_ERR_RUNTIME, "unknown validator type");
     if (E < 0) throw std::invalid_argument("negative edge count");
     HostCst& C = c->c;
+    check_arr(s1, E * C.q_dim(), "s1");
+    check_arr(s2, E * C.q_dim(), "s2");
+    check_arr(out, E, "out");
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
@@ -1925,6 +1953,8 @@ int pmgpu_cst_link_poses(pmgpu_cst* c, int32_t link, const double* q, int64_t B,
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
+    check_arr(out7, B, "out7");
     const int slot = C.slot_for_link(link);
     const PmTablesHdr* T = C.tables();
     const double* st = C.kin->d_state.as<double>();
@@ -1949,8 +1979,9 @@ int pmgpu_ik_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, cons
     check_ptr(c, "cst");
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
-    check_ptr(cost, "cost");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
+    check_arr(cost, B, "cost");
     GradArgs a = grad_args(C, p, target != nullptr);
     a.steps = 0;
     const PmTablesHdr* T = C.tables();
@@ -1985,6 +2016,7 @@ int pmgpu_ik_descend(pmgpu_cst* c, const pmgpu_cost_params* p, float* q, const f
     if (steps < 1) throw std::invalid_argument("steps must be positive");
     if (!std::isfinite(lr)) throw std::invalid_argument("lr must be finite");
     HostCst& C = c->c;
+    check_arr(q, B * C.q_dim(), "q");
     GradArgs a = grad_args(C, p, target != nullptr);
     if (a.mode != PMGPU_COST_SUM) fail(PMGPU_ERR_INVALID, "descent minimises the PMGPU_COST_SUM cost");
     a.steps = steps;
@@ -2021,7 +2053,8 @@ int pmgpu_traj_cost(pmgpu_cst* c, const pmgpu_cost_params* p, const float* q, co
     check_mem(mem);
     if (n_traj < 0 || n_waypoints < 0) throw std::invalid_argument("negative count");
     check_ptr(offsets, "offsets");
-    check_ptr(cost, "cost");
+    check_arr(cost, n_traj, "cost");
+    check_arr(q, n_waypoints * c->c.q_dim(), "q");
     if (mem == PMGPU_MEM_HOST) {  // the device clamps offsets into range; host input is checked
       if (offsets[0] != 0 || offsets[n_traj] != n_waypoints)
         throw std::invalid_argument("offsets must start at 0 and end at n_waypoints");
@@ -2179,6 +2212,7 @@ int pmgpu_posecst_evaluate(pmgpu_posecst* c, const double* q, int64_t B, double*
     check_ptr(c, "constraint");
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
+    check_arr(q, B * c->c.q_dim(), "q");
     const PmPoseTerm* dt = c->device_terms();
     const PmTablesHdr* T = c->c.tables();
     const double* st = c->c.kin->d_state.as<double>();
@@ -2207,6 +2241,8 @@ int pmgpu_posecst_is_valid(pmgpu_posecst* c, const double* q, int64_t B, uint8_t
     check_mem(mem);
     if (B < 0) throw std::invalid_argument("negative batch");
     if (c->equality) fail(PMGPU_ERR_INVALID, "an equality constraint has no is_valid");
+    check_arr(q, B * c->c.q_dim(), "q");
+    check_arr(out, B, "out");
     const PmPoseTerm* dt = c->device_terms();
     const PmTablesHdr* T = c->c.tables();
     const double* st = c->c.kin->d_state.as<double>();

@@ -318,3 +318,71 @@ def test_bench_issue_rate():
     for k, v in per.items():  # the capture's own durations give its issue-active share, roughly
         f = bench.issue_rate(v["warp_instructions"], v["ms"], 2070.0, 152)["frac"]
         assert abs(f * 100 - v["issue_active_pct"]) < 6.0, (k, f)
+
+
+def test_batch_entry_points_refuse_null_arrays():
+    """Every batch entry point of the C ABI refuses a NULL required array of a non-empty batch with
+    PMGPU_ERR_INVALID (in device memory it would fault the kernel that reads it), and a negative
+    count, before any device work; optional outputs stay optional."""
+    import ctypes as C
+
+    from plainmp_gb300 import BaseType, CloudSDF, KinematicModel, LinkPositionBoundCst, _lib, scenes
+    from plainmp_gb300 import workloads as W
+
+    lib = _lib.lib
+    robot = W.chain7_robot()
+    kin, cst, _ = scenes.make_constraint(robot, W.chain7_scene())
+    h = cst._h
+    b = LinkPositionBoundCst(KinematicModel(robot.urdf), robot.control_joints, BaseType.FIXED, robot.end_link, 2, lb=0.1)
+    cloud = CloudSDF(np.zeros((4, 3)), 0.0)
+    q = np.zeros((4, 7))
+    qf = np.zeros((4, 7), np.float32)
+    u8 = np.zeros(16, np.uint8)
+    f64 = np.zeros(64)
+    f32 = np.zeros(64, np.float32)
+    off = np.array([0, 4], np.int64)
+    P = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
+    N = None
+    H = _lib.MEM_HOST
+    cases = {
+        "q": [lambda: lib.pmgpu_cst_is_valid(h, N, 4, P(u8), H, N),
+              lambda: lib.pmgpu_cst_evaluate(h, N, 4, P(f64), P(f64), H, N),
+              lambda: lib.pmgpu_cst_sphere_distances(h, N, 4, 0, P(f64), N, H, N),
+              lambda: lib.pmgpu_cst_is_valid_fast(h, N, 4, P(u8), N, N, H, N),
+              lambda: lib.pmgpu_cst_link_poses(h, 3, N, 4, P(f64), H, N),
+              lambda: lib.pmgpu_posecst_evaluate(b._h, N, 4, P(f64), P(f64), H, N),
+              lambda: lib.pmgpu_posecst_is_valid(b._h, N, 4, P(u8), H, N),
+              lambda: lib.pmgpu_ik_cost(h, N, N, N, 4, P(f32), N, H, N),
+              lambda: lib.pmgpu_ik_descend(h, N, N, N, 4, 1, C.c_float(0.1), 0, N, N, H, N),
+              lambda: lib.pmgpu_traj_cost(h, N, N, P(off), 1, 4, P(f32), N, H, N)],
+        "out": [lambda: lib.pmgpu_cst_is_valid(h, P(q), 4, N, H, N),
+                lambda: lib.pmgpu_cst_is_valid_fast(h, P(q), 4, N, N, N, H, N),
+                lambda: lib.pmgpu_posecst_is_valid(b._h, P(q), 4, N, H, N),
+                lambda: lib.pmgpu_check_motion(h, P(q), P(q), 4, 1, N, 0.1, N, N, H, N),
+                lambda: lib.pmgpu_check_motion_fast(h, P(q), P(q), 4, 1, N, 0.1, N, N, H, N),
+                lambda: lib.pmgpu_sdf_evaluate(cloud._h, P(f64), 4, N, H, N)],
+        "vals": [lambda: lib.pmgpu_cst_evaluate(h, P(q), 4, N, P(f64), H, N)],
+        "jac": [lambda: lib.pmgpu_cst_evaluate(h, P(q), 4, P(f64), N, H, N)],
+        "out7": [lambda: lib.pmgpu_cst_link_poses(h, 3, P(q), 4, N, H, N)],
+        "cost": [lambda: lib.pmgpu_ik_cost(h, N, P(qf), N, 4, N, N, H, N),
+                 lambda: lib.pmgpu_traj_cost(h, N, P(qf), P(off), 1, 4, N, N, H, N)],
+        "s1": [lambda: lib.pmgpu_check_motion(h, N, P(q), 4, 1, N, 0.1, P(u8), N, H, N),
+               lambda: lib.pmgpu_check_motion_fast(h, N, P(q), 4, 1, N, 0.1, P(u8), N, H, N)],
+        "s2": [lambda: lib.pmgpu_check_motion(h, P(q), N, 4, 1, N, 0.1, P(u8), N, H, N)],
+        "points": [lambda: lib.pmgpu_sdf_evaluate(cloud._h, N, 4, P(f64), H, N),
+                   lambda: lib.pmgpu_sdf_is_outside(cloud._h, N, P(f64), 4, P(u8), H, N),
+                   lambda: lib.pmgpu_cloud_nearest(cloud._h, N, 4, P(f64), N, H, N)],
+        "radii": [lambda: lib.pmgpu_sdf_is_outside(cloud._h, P(f64), N, 4, P(u8), H, N)],
+    }
+    for what, calls in cases.items():
+        for i, call in enumerate(calls):
+            rc = call()
+            msg = lib.pmgpu_last_error().decode()
+            assert rc == _lib.PMGPU_ERR_INVALID and msg.endswith(f"{what} is NULL"), (what, i, rc, msg)
+    for call in (lambda: lib.pmgpu_cst_sphere_distances(h, P(q), -1, 0, N, N, H, N),
+                 lambda: lib.pmgpu_check_motion(h, P(q), P(q), -1, 1, N, 0.1, P(u8), N, H, N),
+                 lambda: lib.pmgpu_cloud_nearest(cloud._h, P(f64), -1, N, N, H, N)):
+        assert call() == _lib.PMGPU_ERR_INVALID and "negative" in lib.pmgpu_last_error().decode()
+    # an empty batch needs no arrays; optional outputs may be NULL (the call then reaches the device)
+    assert lib.pmgpu_cst_is_valid(h, N, 0, N, H, N) in (_lib.PMGPU_OK, _lib.PMGPU_ERR_CUDA)
+    assert lib.pmgpu_cst_sphere_distances(h, P(q), 4, 0, N, N, H, N) in (_lib.PMGPU_OK, _lib.PMGPU_ERR_CUDA)
