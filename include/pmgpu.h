@@ -185,7 +185,7 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
                             int mem, void* stream);
 
 /* Launch shape of the fast kernel: configurations per block and threads per block, one of
- * (16,128) (32,128) (32,256) (64,256) (32,512) (64,512) (128,512); chosen per workload by the
+ * (16,128) (32,128) (16,256) (32,256) (64,256) (32,512) (64,512) (128,512); chosen per workload by the
  * autotuner (plainmp_gb300/autotune.py).  No counterpart in the reference. */
 int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block);
 int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* threads_per_block);
