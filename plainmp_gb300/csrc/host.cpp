@@ -1182,14 +1182,9 @@ int pmgpu_model_add_new_link(pmgpu_model* m, const char* name, const char* paren
     else
       set_row(M.state_init, PM_STATE_LINK_ROW(id), qi, xyz, true);
     M.version++;
-    if (M.dev_ready) {
-      M.dev_ready = true;  // ensure_device() re-uploads with the appended row
-      M.ensure_device();
-      const double* r = M.state_init.data() + (size_t)PM_STATE_LINK_ROW(id) * PM_STATE_STRIDE;
-      cuda_check(cudaMemcpy(M.d_state.as<double>() + (size_t)PM_STATE_LINK_ROW(id) * PM_STATE_STRIDE, r, PM_STATE_STRIDE * 8,
-                            cudaMemcpyHostToDevice),
-                 "new link upload");
-    }
+    // a model already on the device grows there: ensure_device() sees the new row count, keeps the
+    // current state of the existing rows and uploads the appended row from state_init
+    if (M.dev_ready) M.ensure_device();
     if (id_out) *id_out = id;
   });
 }

@@ -386,3 +386,26 @@ def test_batch_entry_points_refuse_null_arrays():
     # an empty batch needs no arrays; optional outputs may be NULL (the call then reaches the device)
     assert lib.pmgpu_cst_is_valid(h, N, 0, N, H, N) in (_lib.PMGPU_OK, _lib.PMGPU_ERR_CUDA)
     assert lib.pmgpu_cst_sphere_distances(h, P(q), 4, 0, N, N, H, N) in (_lib.PMGPU_OK, _lib.PMGPU_ERR_CUDA)
+
+
+def test_add_new_link():
+    """KinematicModel.add_new_link (kinematics.cpp:292-338 via kinematic_model_wrapper.cpp:31-39): the
+    new link gets the next id under the given name; a name given twice raises RuntimeError
+    (tests/test_kinematics.py:20-35); an unknown parent raises ValueError (get_link_ids,
+    kinematics.cpp:264-276). Host work only."""
+    from plainmp_gb300 import KinematicModel
+    from plainmp_gb300 import workloads as W
+
+    robot = W.chain7_robot()
+    kin = KinematicModel(robot.urdf)
+    n = kin.num_links
+    i = kin.add_new_link("hahahahah", "link1", [0.1, 0, 0], [0, 0, 0.3], True)
+    assert i == n and kin.num_links == n + 1
+    assert list(kin.get_link_ids(["hahahahah"])) == [i] and kin.link_name(i) == "hahahahah"
+    with pytest.raises(RuntimeError, match="already exists"):
+        kin.add_new_link("hahahahah", "link1", [0, 0, 0], [0, 0, 0], True)
+    with pytest.raises(ValueError, match="no link named"):
+        kin.add_new_link("other", "nolink", [0, 0, 0], [0, 0, 0], True)
+    assert kin.num_links == n + 1
+    j = kin.add_new_link("child_of_new", "hahahahah", [0, 0, 0.2], [0, 0, 0], False)
+    assert j == n + 1
