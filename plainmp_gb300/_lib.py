@@ -196,6 +196,10 @@ class Batch:
         except ImportError:  # pragma: no cover
             pass
         if self.torch is not None and x.is_cuda:
+            cur = self.torch.cuda.current_device()
+            if x.device.index != cur:  # the library's kernels run on the current device
+                raise ValueError(f"the batch is on {x.device} but the current CUDA device is cuda:{cur}: "
+                                 "select its device first (torch.cuda.set_device)")
             tdt = {np.float64: self.torch.float64, np.float32: self.torch.float32, np.uint8: self.torch.uint8,
                    np.int64: self.torch.int64}[dtype]
             self.keep = x.detach().to(tdt).contiguous()

@@ -70,6 +70,22 @@ static void require_device() {
   }
 }
 
+// The CUDA device current on the calling thread.
+static int current_device() {
+  int d = -1;
+  cuda_check(cudaGetDevice(&d), "cudaGetDevice");
+  return d;
+}
+// Device data (model state, constraint tables, cloud grids, SDF images) stay on the device that was
+// current at their first batch call.  A call made while another device is current would hand that
+// device's kernels foreign pointers, so it is refused.
+static void check_device(int owner, const char* what) {
+  const int cur = current_device();
+  if (cur != owner)
+    fail(PMGPU_ERR_INVALID, std::string(what) + " was placed on CUDA device " + std::to_string(owner) +
+                                " by its first batch call, but the calling thread's current device is " + std::to_string(cur));
+}
+
 // ---------------------------------------------------------------------------- kernel timing
 namespace {
 struct ProfRec {
@@ -172,12 +188,15 @@ struct HostModel {
   DevBuf d_scratch;
   int dev_rows = 0;
   bool dev_ready = false;
+  int device = -1;  // the CUDA device holding d_state, d_parents and every constraint's tables
 
   int n_link() const { return (int)link_name.size(); }
 
   void ensure_device() {
+    if (dev_ready) check_device(device, "the kinematic model");
     if (dev_ready && dev_rows == n_link() + 1) return;
     require_device();
+    if (!dev_ready) device = current_device();
     size_t rows = n_link() + 1;
     std::vector<double> host(state_init);
     if (dev_ready && dev_rows > 0) {  // keep the current state when links were appended
@@ -297,6 +316,7 @@ struct CloudData {
   double cell = 0;
   double lb[3], ub[3];
   bool built = false;
+  int device = -1;  // the CUDA device holding the grid
   ~CloudData() {
     if (built) grid_free(g);
   }
@@ -474,11 +494,13 @@ static void check_rotation(const double* rot) {
 struct SdfDeviceImage {
   DevBuf prims, clouds;
   int n_prims = 0;
+  int device = -1;
   std::vector<std::pair<const HostSdf*, uint64_t>> sig;
 };
 
 static void build_cloud(CloudData& cd) {
   require_device();
+  cd.device = current_device();
   int64_t n = (int64_t)(cd.pts.size() / 3);
   DevBuf dpts;
   dpts.ensure(std::max<size_t>(cd.pts.size() * 8, 8));
@@ -530,6 +552,13 @@ static void build_cloud(CloudData& cd) {
   cd.cell = cell;
   cd.d_grid.ensure(sizeof(PmGridDev));
   cuda_check(cudaMemcpy(cd.d_grid.p, &g.dev, sizeof(PmGridDev), cudaMemcpyHostToDevice), "grid descriptor upload");
+}
+// The grid of a cloud, built on first use; later uses must come from the same device.
+static void use_cloud(CloudData& cd) {
+  if (!cd.built)
+    build_cloud(cd);
+  else
+    check_device(cd.device, "a CloudSDF's grid");
 }
 
 // ---------------------------------------------------------------------------- SphereCollisionCst
@@ -757,7 +786,7 @@ struct HostCst {
     for (auto& x : flat) {
       int ci = -1;
       if (x->kind == PM_SDF_CLOUD) {
-        if (!x->cloud->built) build_cloud(*x->cloud);
+        use_cloud(*x->cloud);
         ci = (int)clouds.size();
         clouds.push_back(x->cloud->g.dev);
       }
@@ -898,14 +927,16 @@ const PmPrim* sdf_image(pmgpu_sdf* h, int* n_prims, const PmGridDev** clouds) {
   flatten(h->s, f);
   std::vector<std::pair<const HostSdf*, uint64_t>> sig;
   for (auto& x : f) sig.push_back({x.get(), x->version});
+  if (h->img.prims.p) check_device(h->img.device, "this SDF");
   if (!h->img.prims.p || sig != h->img.sig) {
     require_device();
+    h->img.device = current_device();
     std::vector<PmPrim> prims;
     std::vector<PmGridDev> cl;
     for (auto& x : f) {
       int ci = -1;
       if (x->kind == PM_SDF_CLOUD) {
-        if (!x->cloud->built) build_cloud(*x->cloud);
+        use_cloud(*x->cloud);
         ci = (int)cl.size();
         cl.push_back(x->cloud->g.dev);
       }
@@ -1662,6 +1693,12 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 bool cst_device_view(pmgpu_cst* c, const PmTablesHdr** T, PmTablesHdr* hdr, const double** state, int* cpb, int* nt) {
   HostCst& C = c->c;
   if (!C.d_tables.p || !C.kin->dev_ready || C.sig_model_version != C.kin->version) return false;
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (cur != C.kin->device) return false;  // the tables live on another device
   std::vector<std::shared_ptr<HostSdf>> f;
   if (C.fixed_sdf) flatten(C.fixed_sdf, f);
   if (C.sdf) flatten(C.sdf, f);

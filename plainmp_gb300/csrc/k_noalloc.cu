@@ -59,8 +59,8 @@ extern "C" int pmgpu_cst_is_valid_fast_noalloc(pmgpu_cst* c, const double* q, in
   int cpb = 32, nt = 256;
   if (!pmg::cst_device_view(c, &T, &hdr, &state, &cpb, &nt))
     return fail(PMGPU_ERR_RUNTIME,
-                "pmgpu_cst_is_valid_fast_noalloc: the constraint's tables are not on the device (or the scene changed); "
-                "make one allocating batch call first");
+                "pmgpu_cst_is_valid_fast_noalloc: the constraint's tables are not on the current CUDA device, or the scene "
+                "changed since they were built; make one allocating batch call first, with the model's device current");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();
