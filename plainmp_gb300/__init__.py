@@ -3,12 +3,13 @@
 Batched forward kinematics, sphere-vs-SDF checks (box, sphere, cylinder, ground, point
 cloud), self-collision sphere pairs, motion-validator edge checks and constraint Jacobians,
 as hand-written sm_103a CUDA kernels behind the C ABI in include/pmgpu.h.  The Python
-modules mirror the reference's ``plainmp.kinematics``, ``plainmp.psdf`` and
-``plainmp.constraint`` interfaces.
+modules mirror the reference's ``plainmp.kinematics``, ``plainmp.psdf``, ``plainmp.constraint``
+and ``plainmp.kdtree`` interfaces.
 """
 from ._lib import CudaError, DeviceTimeout, device_count  # noqa: F401
 from .constraint import (EqCompositeCst, IneqCompositeCst, LinkPoseCst, LinkPositionBoundCst,  # noqa: F401
-                         SphereAttachmentSpec, SphereCollisionCst)
+                         SequentialCst, SphereAttachmentSpec, SphereCollisionCst)
+from .kdtree import KDTree  # noqa: F401
 from .kinematics import BaseType, KinematicModel  # noqa: F401
 from .motion_validator import BoxMotionValidator, EuclideanMotionValidator  # noqa: F401
 from .psdf import BoxSDF, CloudSDF, CylinderSDF, GroundSDF, Pose, SDFBase, SphereSDF, UnionSDF  # noqa: F401

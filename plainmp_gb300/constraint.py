@@ -377,3 +377,7 @@ class IneqCompositeCst(_CompositeBase):
 
     def is_valid(self, q) -> bool:
         return bool(self.is_valid_batch(f64(q, (1, self.q_dim())))[0])
+
+
+# plainmp.constraint also holds SequentialCst (bindings/constraint.cpp:114-125)
+from .sequential import SequentialCst  # noqa: E402,F401

@@ -409,3 +409,23 @@ def test_add_new_link():
     assert kin.num_links == n + 1
     j = kin.add_new_link("child_of_new", "hahahahah", [0, 0, 0.2], [0, 0, 0], False)
     assert j == n + 1
+
+
+def test_kdtree_and_module_layout():
+    """plainmp.kdtree.KDTree (bindings/kdtree.cpp:20-23) and plainmp.constraint.SequentialCst
+    (bindings/constraint.cpp:114-125) are where the reference's modules have them; an empty KDTree
+    answers sqdist with the largest double, as kdtree.cpp:33-38 does; a query is one 3-vector."""
+    import plainmp_gb300 as pm
+    from plainmp_gb300.constraint import SequentialCst
+    from plainmp_gb300.kdtree import KDTree
+
+    assert pm.KDTree is KDTree and pm.SequentialCst is SequentialCst
+    empty = KDTree(np.zeros((0, 3)))
+    assert len(empty) == 0 and empty.sqdist([0.0, 0.0, 0.0]) == np.finfo(np.float64).max
+    assert np.isnan(empty.query([1.0, 2.0, 3.0])).all()
+    tree = KDTree([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]])  # a list of 3-vectors, as the reference takes
+    assert len(tree) == 2
+    with pytest.raises(ValueError):
+        tree.query([1.0, 2.0])
+    with pytest.raises(ValueError):
+        KDTree(np.zeros((4, 2)))

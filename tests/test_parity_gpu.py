@@ -211,6 +211,22 @@ def test_cloud_nearest_cell_sizes(oracle, cell):
         assert np.array_equal(mine.is_outside_points(q, r), ref.is_outside(q, r))
 
 
+def test_kdtree_vs_brute_force():  # tests/test_kdtree.py:6-20
+    from plainmp_gb300 import KDTree
+
+    rng = np.random.default_rng(0)
+    points = rng.standard_normal((1000, 3))
+    tree = KDTree(points)
+    Q = rng.standard_normal((1000, 3))
+    for q in Q[:200]:  # one query per call, as the reference's test makes them
+        nearest = tree.query(q)
+        assert np.allclose(nearest, points[np.argmin(np.sum((points - q) ** 2, axis=1))])
+        assert np.allclose(np.sum((nearest - q) ** 2), tree.sqdist(q))
+    idx = np.argmin(((points[None, :, :] - Q[:, None, :]) ** 2).sum(-1), axis=1)
+    np.testing.assert_array_equal(tree.query_batch(Q), points[idx])  # the set's own coordinates
+    np.testing.assert_allclose(tree.sqdist_batch(Q), ((points[idx] - Q) ** 2).sum(-1), rtol=1e-12, atol=0)
+
+
 def test_cloud_edge_cases(oracle):
     from plainmp_gb300 import CloudSDF
 
