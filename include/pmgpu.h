@@ -232,6 +232,9 @@ int pmgpu_linkbound_create(pmgpu_model* kin, const char* const* control_joints, 
 void pmgpu_posecst_destroy(pmgpu_posecst* c);
 /* q_dim, cst_dim and whether the constraint is an equality (LinkPoseCst) */
 int pmgpu_posecst_dims(const pmgpu_posecst* c, int* q_dim, int* cst_dim, int* is_equality);
+/* ConstraintBase::update_kintree(q, high_accuracy) (constraints/primitive.hpp:38-62;
+ * bindings/constraint.cpp:31-32) on the shared model state, as pmgpu_cst_update_kintree. */
+int pmgpu_posecst_update_kintree(pmgpu_posecst* c, const double* q, int high_accuracy);
 /* ConstraintBase::evaluate(q) (constraints/primitive.hpp:74-79) for B configurations, FP64:
  * vals B x cst_dim, jac B x cst_dim x q_dim (row-major), either may be NULL.  The rows follow
  * get_jacobian (kinematics/algorithm.cpp:212-344) with RotationType IGNORE / RPY / XYZW. */

@@ -109,6 +109,7 @@ _SIGS = {
     "pmgpu_linkbound_create": (_i, [_p, _cpp, _i, _i, C.c_char_p, _i, _i, _d, _i, _d, C.POINTER(_p)]),
     "pmgpu_posecst_destroy": (None, [_p]),
     "pmgpu_posecst_dims": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    "pmgpu_posecst_update_kintree": (_i, [_p, _dp, _i]),
     "pmgpu_posecst_evaluate": (_i, [_p, _p, _i64, _p, _p, _i, _p]),
     "pmgpu_posecst_is_valid": (_i, [_p, _p, _i64, _p, _i, _p]),
     "pmgpu_ik_cost": (_i, [_p, _p, _p, _p, _i64, _p, _p, _i, _p]),

@@ -241,6 +241,11 @@ class _PoseCstBase:
     def get_control_joint_names(self) -> List[str]:
         return list(self.control_joint_names)
 
+    def update_kintree(self, q, high_accuracy: bool = True) -> None:
+        """ConstraintBase.update_kintree (primitive.hpp:38-62) on the shared model state."""
+        qq = f64(q, (self.q_dim(),))
+        check(lib.pmgpu_posecst_update_kintree(self._h, dptr(qq), int(bool(high_accuracy))))
+
     def _batch(self, Q):
         b = Batch(Q)
         if len(b.shape) != 2 or b.shape[1] != self.q_dim():

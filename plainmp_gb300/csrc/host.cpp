@@ -1583,21 +1583,31 @@ int pmgpu_cst_groups(const pmgpu_cst* c, int32_t* link, double* radius, double* 
     }
   });
 }
+}  // extern "C"
+
+// ConstraintBase::update_kintree(q, high_accuracy) (primitive.hpp:38-62) on the shared model state:
+// the control joints, then the base for PLANAR / FLOATING bases, whose joints always use exact
+// sin/cos.
+static void update_kintree_of(HostCst& C, const double* q, int high_accuracy) {
+  check_arr(q, C.q_dim(), "q");
+  C.tables();
+  HostModel& M = *C.kin;
+  int nq = C.q_dim(), nc = (int)C.ids.size();
+  for (int i = 0; i < nc; i++) M.angles[C.ids[i]] = q[i];
+  double* dq = (double*)C.w_aux.ensure((size_t)nq * 8 + 16);
+  cuda_check(cudaMemcpy(dq, q, (size_t)nq * 8, cudaMemcpyHostToDevice), "H2D");
+  int accurate = (C.base_type != PM_BASE_FIXED) ? 1 : (high_accuracy ? 1 : 0);
+  if (nc > 0) cuda_check(launch_set_joints(M.d_state.as<double>(), C.d_ctrl_recs.as<PmSlot>(), dq, nc, accurate, 0), "update_kintree");
+  if (C.base_type != PM_BASE_FIXED) cuda_check(launch_set_base_from_q(M.d_state.as<double>(), C.base_type, dq + nc, 0), "update_kintree");
+  cuda_check(cudaDeviceSynchronize(), "update_kintree");
+}
+
+extern "C" {
+
 int pmgpu_cst_update_kintree(pmgpu_cst* c, const double* q, int high_accuracy) {
   return guarded([&] {
     check_ptr(c, "cst");
-    HostCst& C = c->c;
-    C.tables();
-    HostModel& M = *C.kin;
-    int nq = C.q_dim(), nc = (int)C.ids.size();
-    for (int i = 0; i < nc; i++) M.angles[C.ids[i]] = q[i];
-    double* dq = (double*)C.w_aux.ensure((size_t)nq * 8 + 16);
-    cuda_check(cudaMemcpy(dq, q, (size_t)nq * 8, cudaMemcpyHostToDevice), "H2D");
-    // primitive.hpp:38-62: non-FIXED bases always use exact sin/cos for the joints
-    int accurate = (C.base_type != PM_BASE_FIXED) ? 1 : (high_accuracy ? 1 : 0);
-    if (nc > 0) cuda_check(launch_set_joints(M.d_state.as<double>(), C.d_ctrl_recs.as<PmSlot>(), dq, nc, accurate, 0), "update_kintree");
-    if (C.base_type != PM_BASE_FIXED) cuda_check(launch_set_base_from_q(M.d_state.as<double>(), C.base_type, dq + nc, 0), "update_kintree");
-    cuda_check(cudaDeviceSynchronize(), "update_kintree");
+    update_kintree_of(c->c, q, high_accuracy);
   });
 }
 static int spheres_of_state(pmgpu_cst* c, double* out4, int groups) {
@@ -2236,6 +2246,13 @@ int pmgpu_posecst_dims(const pmgpu_posecst* c, int* q_dim, int* cst_dim, int* is
     if (q_dim) *q_dim = c->c.q_dim();
     if (cst_dim) *cst_dim = c->cst_dim;
     if (is_equality) *is_equality = c->equality ? 1 : 0;
+  });
+}
+
+int pmgpu_posecst_update_kintree(pmgpu_posecst* c, const double* q, int high_accuracy) {
+  return guarded([&] {
+    check_ptr(c, "constraint");
+    update_kintree_of(c->c, q, high_accuracy);
   });
 }
 

@@ -354,7 +354,9 @@ def test_batch_entry_points_refuse_null_arrays():
               lambda: lib.pmgpu_posecst_is_valid(b._h, N, 4, P(u8), H, N),
               lambda: lib.pmgpu_ik_cost(h, N, N, N, 4, P(f32), N, H, N),
               lambda: lib.pmgpu_ik_descend(h, N, N, N, 4, 1, C.c_float(0.1), 0, N, N, H, N),
-              lambda: lib.pmgpu_traj_cost(h, N, N, P(off), 1, 4, P(f32), N, H, N)],
+              lambda: lib.pmgpu_traj_cost(h, N, N, P(off), 1, 4, P(f32), N, H, N),
+              lambda: lib.pmgpu_cst_update_kintree(h, N, 1),
+              lambda: lib.pmgpu_posecst_update_kintree(b._h, N, 1)],
         "out": [lambda: lib.pmgpu_cst_is_valid(h, P(q), 4, N, H, N),
                 lambda: lib.pmgpu_cst_is_valid_fast(h, P(q), 4, N, N, N, H, N),
                 lambda: lib.pmgpu_posecst_is_valid(b._h, P(q), 4, N, H, N),

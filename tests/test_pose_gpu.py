@@ -144,3 +144,19 @@ def test_ineq_composite(oracle):
     v2, j2 = b.evaluate_batch(Q[:16])
     assert np.array_equal(vals, np.concatenate([v1, v2], axis=1)) and np.array_equal(jac, np.concatenate([j1, j2], axis=1))
     assert comp.is_valid(Q[0]) == bool(ref[0])
+
+
+def test_pose_constraint_update_kintree():
+    """ConstraintBase.update_kintree of a pose constraint (bindings/constraint.cpp:31-32) sets the
+    shared model exactly as the collision constraint's does (primitive.hpp:38-62)."""
+    robot = W.chain7_robot()
+    kin, cst, _ = scenes.make_constraint(robot, W.chain7_scene())
+    b = LinkPositionBoundCst(kin, robot.control_joints, BaseType.FIXED, robot.end_link, 2, lb=0.1)
+    q = W.chain7_configs(2, seed=7)
+    for high_accuracy in (True, False):
+        cst.update_kintree(q[0], high_accuracy)
+        ref = kin.debug_get_link_pose(robot.end_link)
+        cst.update_kintree(q[1], high_accuracy)
+        b.update_kintree(q[0], high_accuracy)
+        np.testing.assert_array_equal(kin.debug_get_link_pose(robot.end_link), ref)
+        np.testing.assert_array_equal(kin.get_joint_positions(kin.get_joint_ids(robot.control_joints)), q[0])
