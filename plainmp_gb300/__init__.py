@@ -7,11 +7,13 @@ modules mirror the reference's ``plainmp.kinematics``, ``plainmp.psdf``, ``plain
 and ``plainmp.kdtree`` interfaces.
 """
 from ._lib import CudaError, DeviceTimeout, device_count  # noqa: F401
-from .constraint import (EqCompositeCst, IneqCompositeCst, LinkPoseCst, LinkPositionBoundCst,  # noqa: F401
-                         SequentialCst, SphereAttachmentSpec, SphereCollisionCst)
+from .constraint import (ConstraintBase, EqCompositeCst, EqConstraintBase, IneqCompositeCst,  # noqa: F401
+                         IneqConstraintBase, LinkPoseCst, LinkPositionBoundCst, SequentialCst, SphereAttachmentSpec,
+                         SphereCollisionCst)
 from .kdtree import KDTree  # noqa: F401
 from .kinematics import BaseType, KinematicModel  # noqa: F401
 from .motion_validator import BoxMotionValidator, EuclideanMotionValidator  # noqa: F401
-from .psdf import BoxSDF, CloudSDF, CylinderSDF, GroundSDF, Pose, SDFBase, SphereSDF, UnionSDF  # noqa: F401
+from .psdf import (BoxSDF, ClosedPrimitiveSDFBase, CloudSDF, CylinderSDF, GroundSDF, Pose,  # noqa: F401
+                   PrimitiveSDFBase, SDFBase, SphereSDF, UnionSDF)
 
 __version__ = "0.1.0"

@@ -19,6 +19,21 @@ from .kinematics import BaseType, KinematicModel
 from .psdf import SDFBase
 
 
+class ConstraintBase:
+    """plainmp.constraint.ConstraintBase (bindings/constraint.cpp:31-35): update_kintree(q,
+    high_accuracy), evaluate(q) -> (values, jacobian), get_kin(), get_control_joint_names().  Every
+    constraint below provides them; the *_batch methods are the batched forms."""
+
+
+class EqConstraintBase(ConstraintBase):
+    """plainmp.constraint.EqConstraintBase (bindings/constraint.cpp:36-37): values meant to be zero."""
+
+
+class IneqConstraintBase(ConstraintBase):
+    """plainmp.constraint.IneqConstraintBase (bindings/constraint.cpp:38-39): values meant to be
+    non-negative, with is_valid(q)."""
+
+
 @dataclass
 class SphereAttachmentSpec:
     """SphereAttachmentSpec(parent_link_name, relative_positions (3, n), radii (n,), only_self_collision)."""
@@ -37,7 +52,7 @@ class SphereAttachmentSpec:
             raise ValueError("relative_positions and radii disagree on the sphere count")
 
 
-class SphereCollisionCst:
+class SphereCollisionCst(IneqConstraintBase):
     def __init__(self, kin: KinematicModel, control_joint_names: Sequence[str], base_type: BaseType,
                  sphere_specs: Sequence[SphereAttachmentSpec], selcol_pairs: Sequence[Tuple[str, str]],
                  fixed_sdf: Optional[SDFBase] = None, reorder_spheres: bool = True) -> None:
@@ -267,7 +282,7 @@ class _PoseCstBase:
         return vals[0], jac[0]
 
 
-class LinkPoseCst(_PoseCstBase):
+class LinkPoseCst(_PoseCstBase, EqConstraintBase):
     """LinkPoseCst(kin, control_joint_names, base_type, link_names, poses): poses of 3 (position),
     6 (position + RPY) or 7 (position + quaternion xyzw) values (constraints/primitive_link_pose.cpp)."""
 
@@ -289,7 +304,7 @@ class LinkPoseCst(_PoseCstBase):
         return [p.copy() for p in self._poses]
 
 
-class LinkPositionBoundCst(_PoseCstBase):
+class LinkPositionBoundCst(_PoseCstBase, IneqConstraintBase):
     """LinkPositionBoundCst(kin, control_joint_names, base_type, link_name, axis, lb, ub): lb <= p[axis] <= ub
     for the link's world position, either bound optional (constraints/primitive_link_position_bound.cpp)."""
 
@@ -319,10 +334,15 @@ class _CompositeBase:
     The reference drives the shared model with the first member's q mapping; the batched path
     requires every member to have the same control joints and base type, so the mappings agree."""
 
+    _member = ConstraintBase
+
     def __init__(self, constraints):
         self.constraints = list(constraints)
         if not self.constraints:
             raise ValueError("a composite constraint needs at least one constraint")
+        for c in self.constraints:  # the reference binds the member type (bindings/constraint.cpp:105, 109)
+            if not isinstance(c, self._member):
+                raise TypeError(f"{type(self).__name__} takes {self._member.__name__} members, got {type(c).__name__}")
         k0 = self.constraints[0].get_kin()
         for c in self.constraints:
             if c.get_kin() is not k0:
@@ -363,10 +383,14 @@ def _is_torch(x) -> bool:
 class EqCompositeCst(_CompositeBase):
     """EqCompositeCst(constraints) of equality constraints (LinkPoseCst)."""
 
+    _member = EqConstraintBase
+
 
 class IneqCompositeCst(_CompositeBase):
     """IneqCompositeCst(constraints): is_valid = AND over the members after update_kintree(q, False)
     (composite_constraint.hpp:98-105)."""
+
+    _member = IneqConstraintBase
 
     def is_valid_batch(self, Q, fast: bool = True):
         """(B,) uint8 AND of the members' validity; SphereCollisionCst members use the FP32 +

@@ -123,6 +123,11 @@ class PrimitiveSDFBase(SDFBase):
         return self._info()[2]
 
 
+class ClosedPrimitiveSDFBase(PrimitiveSDFBase):
+    """plainmp.psdf.ClosedPrimitiveSDFBase: the bounded primitives (box, cylinder, sphere), which
+    carry a pose."""
+
+
 class _HasPose:
     @property
     def pose(self) -> Pose:
@@ -130,7 +135,7 @@ class _HasPose:
         return Pose(pos, rot)
 
 
-class BoxSDF(PrimitiveSDFBase, _HasPose):
+class BoxSDF(ClosedPrimitiveSDFBase, _HasPose):
     def __init__(self, size, pose: Optional[Pose] = None) -> None:
         pose = pose or Pose()
         h = C.c_void_p()
@@ -140,7 +145,7 @@ class BoxSDF(PrimitiveSDFBase, _HasPose):
         self._members = []
 
 
-class CylinderSDF(PrimitiveSDFBase, _HasPose):
+class CylinderSDF(ClosedPrimitiveSDFBase, _HasPose):
     def __init__(self, radius: float, height: float, pose: Optional[Pose] = None) -> None:
         pose = pose or Pose()
         h = C.c_void_p()
@@ -150,7 +155,7 @@ class CylinderSDF(PrimitiveSDFBase, _HasPose):
         self._members = []
 
 
-class SphereSDF(PrimitiveSDFBase, _HasPose):
+class SphereSDF(ClosedPrimitiveSDFBase, _HasPose):
     def __init__(self, radius: float, pose: Optional[Pose] = None) -> None:
         pose = pose or Pose()
         h = C.c_void_p()

@@ -431,3 +431,31 @@ def test_kdtree_and_module_layout():
         tree.query([1.0, 2.0])
     with pytest.raises(ValueError):
         KDTree(np.zeros((4, 2)))
+
+
+def test_class_hierarchy_matches_reference():
+    """The reference's base classes (psdf.pyi:36-109, constraint.pyi:9-113): isinstance checks of
+    user code hold, and a composite refuses members of the other kind, as the bound member types
+    do (bindings/constraint.cpp:105, 109)."""
+    import plainmp_gb300 as pm
+    from plainmp_gb300 import workloads as W
+
+    for cls in (pm.BoxSDF, pm.CylinderSDF, pm.SphereSDF):
+        assert issubclass(cls, pm.ClosedPrimitiveSDFBase) and issubclass(cls, pm.PrimitiveSDFBase)
+    for cls in (pm.GroundSDF, pm.CloudSDF):
+        assert issubclass(cls, pm.PrimitiveSDFBase) and not issubclass(cls, pm.ClosedPrimitiveSDFBase)
+    assert issubclass(pm.UnionSDF, pm.SDFBase) and not issubclass(pm.UnionSDF, pm.PrimitiveSDFBase)
+    assert issubclass(pm.SphereCollisionCst, pm.IneqConstraintBase)
+    assert issubclass(pm.LinkPositionBoundCst, pm.IneqConstraintBase)
+    assert issubclass(pm.LinkPoseCst, pm.EqConstraintBase)
+    assert issubclass(pm.EqConstraintBase, pm.ConstraintBase) and issubclass(pm.IneqConstraintBase, pm.ConstraintBase)
+    robot = W.chain7_robot()
+    kin = pm.KinematicModel(robot.urdf)
+    j = robot.control_joints
+    pose = pm.LinkPoseCst(kin, j, pm.BaseType.FIXED, [robot.end_link], [np.zeros(3)])
+    bound = pm.LinkPositionBoundCst(kin, j, pm.BaseType.FIXED, robot.end_link, 2, lb=0.1)
+    assert pm.EqCompositeCst([pose]).cst_dim() == 3 and pm.IneqCompositeCst([bound]).cst_dim() == 1
+    with pytest.raises(TypeError):
+        pm.EqCompositeCst([bound])
+    with pytest.raises(TypeError):
+        pm.IneqCompositeCst([pose])
