@@ -154,8 +154,21 @@ def cpu_baseline(robot, scene, q, seconds: float = 6.0):
         oc.is_valid(q[off:off + n], threads=threads)
         done += n
     dt = time.perf_counter() - t0
-    return {"value": done / dt, "unit": "configs/s", "cores": threads, "kind": "port",
-            "sample": f"{done} configs of the same batch ({reps} x {n}), validity only (the reference has no per-sphere distance output)"}
+    out = {"value": done / dt, "unit": "configs/s", "cores": threads, "kind": "port",
+           "sample": f"{done} configs of the same batch ({reps} x {n}), validity only (the reference has no per-sphere distance output)"}
+    # one core, as one planner process runs the reference's is_valid loop
+    n1 = 1024
+    t0 = time.perf_counter()
+    oc.is_valid(q[:n1], threads=1)
+    dt = time.perf_counter() - t0
+    reps = max(1, min(32, int(seconds / 3 / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    for r in range(reps):
+        off = (r * n1) % (B - n1)
+        oc.is_valid(q[off:off + n1], threads=1)
+    dt = time.perf_counter() - t0
+    out["single_core"] = {"value": reps * n1 / dt, "unit": "configs/s", "cores": 1, "sample": f"{reps * n1} configs ({reps} x {n1})"}
+    return out
 
 
 C0_FLOP = 7 * 90 + 8 * 24 + 56 * 18 + 56 * (35 * 10 + 11 * 5 + 30 * 5) + 960 * 11  # per configuration, the counting rule
@@ -601,11 +614,12 @@ def main():
     alg_bytes = B * (cst.q_dim() * 8 + 1 + ns * 4)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     prof = ROOT / "profiles" / "k_fast_valid_dualarm65536.traffic.json"
-    traffic, issue, inst = None, None, {}
+    traffic, issue, inst, l2 = None, None, {}, None
     if prof.exists():
         pj = json.loads(prof.read_text())
         traffic, issue = pj.get("dram_bytes_per_launch"), pj.get("issue_active_pct")
         inst = {k: v.get("warp_instructions") for k, v in pj.get("per_kernel", {}).items()}
+        l2 = pj.get("l2_bytes_per_launch")
     clocks = clk.summary()
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     k_each = {"k_fast_valid": k_ms / max(k_n, 1), "k_hard_queries": h_ms / max(h_n, 1)}
@@ -654,7 +668,11 @@ def main():
                                         "k_fast_recheck": r_ms / max(r_n, 1)},
                      "note": "HBM is not the binding resource: the kernel is issue/latency bound"
                              + (f" (ncu: SM issue active {issue} %, profiles/k_fast_valid_dualarm65536.md)" if issue else ""),
-                     "issue": issue_step},
+                     "issue": issue_step,
+                     "l2": None if not l2 else {"bytes": l2, "achieved_gbs": l2 / (kernel_ms / 1e3) / 1e9,
+                                                "sector_pct_of_peak_ncu": {k: v.get("l2_sector_pct_of_peak")
+                                                                           for k, v in pj.get("per_kernel", {}).items()},
+                                                "bytes_from": "ncu lts__t_sectors.sum x 32 B of one launch of each kernel"}},
         "clocks": clocks,
         "plain_fp64": {"value": B / (ms_plain / 1e3), "unit": "configs/s", "ms_per_batch": ms_plain,
                        "what": "plain FP64 method, one thread per configuration, validity only"},

@@ -459,3 +459,18 @@ def test_class_hierarchy_matches_reference():
         pm.EqCompositeCst([bound])
     with pytest.raises(TypeError):
         pm.IneqCompositeCst([pose])
+
+
+def test_bench_cpu_baseline_rows():
+    """bench.py's cpu_baseline: the oracle on all host cores and on one core, over bounded samples
+    of the headline batch (a short budget here)."""
+    import sys
+
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    robot, scene, q = bench.workload()
+    cb = bench.cpu_baseline(robot, scene, q, seconds=0.3)
+    assert cb["value"] > 0 and cb["cores"] >= 1 and cb["kind"] == "port"
+    assert cb["single_core"]["value"] > 0 and cb["single_core"]["cores"] == 1
+    assert cb["value"] >= 0.5 * cb["single_core"]["value"]
