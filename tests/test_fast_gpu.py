@@ -60,6 +60,23 @@ def test_fast_dualarm_cloud(dual):
     assert np.array_equal(got, cst.is_valid_batch(Q))
 
 
+def test_fast_dualarm_full_batch(dual):
+    """The benchmark's own batch (65,536 configurations against the 200k-point cloud) through the
+    host-memory call (two-stream chunks): fast validity equals the plain FP64 method's on every
+    configuration, in both modes; the plain method equals the oracle on a strided sample; every
+    FP32 distance is finite, at most the cutoff and within the bound of the FP64 value on a sample."""
+    (_, cst, _), (_, oc, _) = dual
+    Q = W.dualarm_configs(65536)
+    plain = cst.is_valid_batch(Q)
+    ok, d32 = cst.is_valid_fast(Q, distances=True)
+    assert np.array_equal(ok, plain)
+    assert np.array_equal(cst.is_valid_fast(Q), plain)
+    assert np.array_equal(plain[::32], oc.is_valid(Q[::32], threads=8))
+    assert d32.shape == (65536, cst.n_spheres) and np.isfinite(d32).all() and (d32 <= np.float32(CUTOFF)).all()
+    ref = np.minimum(cst.sphere_distances(Q[::64]), CUTOFF)
+    assert np.abs(d32[::64].astype(np.float64) - ref).max() < DIST_TOL
+
+
 def test_fast_dualarm_cloud_distances(dual):
     (_, cst, _), (_, oc, _) = dual
     Q = W.dualarm_configs(8, seed=7)
