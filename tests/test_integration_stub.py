@@ -1,7 +1,10 @@
-"""The pybind11 binding shown in INTEGRATION.md compiles against include/pmgpu.h, links to the
-in-tree library and works: it is built here from the document's own text.  Without a GPU its
-is_valid_batch reports the library's "no CUDA device" error; with one it equals the Python
-mirror's plain method.  Needs pybind11 and g++ (skipped where pybind11 is absent)."""
+"""The bindings shown in INTEGRATION.md, built from the document's own text.
+
+* The pybind11 binding compiles against include/pmgpu.h, links to the in-tree library and works.
+  Without a GPU its is_valid_batch reports the library's "no CUDA device" error; with one it equals
+  the Python mirror's plain method.  Needs pybind11 (skipped where it is absent).
+* The OMPL adapter compiles against include/pmgpu.h and a stand-in of the OMPL declarations it uses.
+"""
 import importlib.util
 import subprocess
 import sys
@@ -70,3 +73,50 @@ def test_pybind11_stub_builds_and_runs(stub):
         return
     _, mine, _ = scenes.make_constraint(robot, W.Scene(), True, True)  # same spheres and pairs, no SDF
     assert np.array_equal(c.is_valid_batch(Q), mine.is_valid_batch(Q))
+
+
+# The OMPL declarations the adapter of INTEGRATION.md section 3 uses (OMPL itself is not installed):
+# State::as<T>(), RealVectorStateSpace::StateType::values, MotionValidator's constructor and its two
+# pure checkMotion overloads, SpaceInformationPtr.
+OMPL_DECLS = """#include <memory>
+#include <stdexcept>
+#include <utility>
+#include <vector>
+namespace ompl { namespace base {
+class State {
+ public:
+  virtual ~State() = default;
+  template <class T> const T* as() const { return static_cast<const T*>(this); }
+  template <class T> T* as() { return static_cast<T*>(this); }
+};
+class RealVectorStateSpace {
+ public:
+  class StateType : public State { public: double* values = nullptr; };
+};
+class SpaceInformation {};
+using SpaceInformationPtr = std::shared_ptr<SpaceInformation>;
+class MotionValidator {
+ public:
+  explicit MotionValidator(const SpaceInformationPtr& si) : si_(si) {}
+  virtual ~MotionValidator() = default;
+  virtual bool checkMotion(const State* s1, const State* s2) const = 0;
+  virtual bool checkMotion(const State* s1, const State* s2, std::pair<State*, double>& last_valid) const = 0;
+ protected:
+  SpaceInformationPtr si_;
+};
+}}  // namespace ompl::base
+"""
+
+
+def test_ompl_adapter_compiles(tmp_path):
+    """INTEGRATION.md's OMPL adapter compiles against include/pmgpu.h (its ABI calls have the
+    header's argument lists) and implements both checkMotion overloads."""
+    text = (REPO / "INTEGRATION.md").read_text()
+    sec = text[text.index("## 3. C++ (OMPL"):]
+    start = sec.index("```cpp\n") + len("```cpp\n")
+    src = tmp_path / "adapter.cpp"
+    src.write_text(OMPL_DECLS + sec[start:sec.index("```", start)] +
+                   "\nint main() { GpuBoxMotionValidator v(nullptr, nullptr, {0.05}); (void)v; return 0; }\n")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", f"-I{REPO / 'include'}", str(src)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-3000:]
