@@ -4,6 +4,7 @@
   Without a GPU its is_valid_batch reports the library's "no CUDA device" error; with one it equals
   the Python mirror's plain method.  Needs pybind11 (skipped where it is absent).
 * The OMPL adapter compiles against include/pmgpu.h and a stand-in of the OMPL declarations it uses.
+* A C99 program includes the header, links to the library and calls it (the ABI is plain C).
 """
 import importlib.util
 import subprocess
@@ -120,3 +121,73 @@ def test_ompl_adapter_compiles(tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", f"-I{REPO / 'include'}", str(src)],
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "pmgpu.h"
+
+static char* slurp(const char* path) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return NULL;
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  char* s = (char*)malloc((size_t)n + 1);
+  if (fread(s, 1, (size_t)n, f) != (size_t)n) n = 0;
+  s[n] = 0;
+  fclose(f);
+  return s;
+}
+
+int main(int argc, char** argv) {
+  char* urdf = argc > 1 ? slurp(argv[1]) : NULL;
+  pmgpu_model* kin = NULL;
+  if (!urdf || pmgpu_model_create(urdf, &kin) != PMGPU_OK) return 10;
+  const char* joints[7] = {"j1", "j2", "j3", "j4", "j5", "j6", "j7"};
+  const char* links[1] = {"link7"};
+  const int32_t counts[1] = {1};
+  const double rel[3] = {0.0, 0.0, 0.0}, radii[1] = {0.05};
+  const uint8_t only[1] = {0};
+  pmgpu_cst* cst = NULL;
+  if (pmgpu_cst_create(kin, joints, 7, PMGPU_BASE_FIXED, 1, links, counts, rel, radii, only, 0, NULL, NULL, NULL, 1, &cst) != PMGPU_OK)
+    return 11;
+  pmgpu_model_destroy(kin); /* the constraint keeps its model */
+  int q_dim = 0, cst_dim = -1, ns = 0, ng = 0;
+  if (pmgpu_cst_dims(cst, &q_dim, &cst_dim, &ns, &ng) != PMGPU_OK) return 12;
+  double q[7] = {0, 0, 0, 0, 0, 0, 0};
+  uint8_t ok = 7;
+  const int rc = pmgpu_cst_is_valid(cst, q, 1, &ok, PMGPU_MEM_HOST, NULL);
+  const int rc_null = pmgpu_cst_is_valid(cst, NULL, 1, &ok, PMGPU_MEM_HOST, NULL);
+  printf("%d %d %d %d %d %d %d %s\n", q_dim, cst_dim, ns, ng, rc, (int)ok, rc_null, pmgpu_last_error());
+  pmgpu_cst_destroy(cst);
+  free(urdf);
+  return 0;
+}
+"""
+
+
+def test_c_caller(tmp_path):
+    """A C99 program includes the header, links to the library and calls it: model and constraint
+    construction, dimensions, is_valid (PMGPU_ERR_CUDA without a GPU, a valid configuration with
+    one: no SDF and no self pairs) and the NULL-argument error."""
+    import plainmp_gb300 as pm
+    from plainmp_gb300 import workloads as W
+
+    (tmp_path / "caller.c").write_text(C_CALLER)
+    (tmp_path / "chain7.urdf").write_text(W.chain7_robot().urdf)
+    lib_dir = REPO / "plainmp_gb300"
+    exe = tmp_path / "caller"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", f"-I{REPO / 'include'}", str(tmp_path / "caller.c"),
+                        "-o", str(exe), f"-L{lib_dir}", "-lpmgpu", f"-Wl,-rpath,{lib_dir}"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(exe), str(tmp_path / "chain7.urdf")], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+    f = r.stdout.split(" ", 7)
+    assert f[:4] == ["7", "0", "1", "1"]  # q_dim, cst_dim (no SDF, no pairs), spheres, groups
+    if pm.device_count() == 0:
+        assert int(f[4]) == 3  # PMGPU_ERR_CUDA
+    else:
+        assert int(f[4]) == 0 and f[5] == "1"
+    assert int(f[6]) == 1 and f[7].strip() == "q is NULL"  # PMGPU_ERR_INVALID
