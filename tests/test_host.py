@@ -463,7 +463,7 @@ def test_class_hierarchy_matches_reference():
 
 def test_bench_cpu_baseline_rows():
     """bench.py's cpu_baseline: the oracle on all host cores and on one core, over bounded samples
-    of the headline batch (a short budget here)."""
+    of the headline batch (a short time limit here)."""
     import sys
 
     sys.path.insert(0, str(REPO))
