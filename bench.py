@@ -116,6 +116,72 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class NvmlPoller:
+    """SM clock and clock-event reasons read from NVML (the library nvidia-smi reads) every ~1 ms
+    in a thread: a timed region of a few tens of ms gets many samples, where nvidia-smi's 200 ms
+    period gets one or two.  Read-only queries; summary() is None when NVML cannot be loaded."""
+
+    # nvmlClocksEventReason bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int, uuid: str = "", period_s: float = 0.001):
+        self.index, self.period = index, period_s
+        self.uuid = uuid if not uuid or uuid.startswith("GPU-") else "GPU-" + uuid  # NVML's form of the CUDA device's UUID
+        self.samples, self.max_mhz, self.lib, self.dev = [], None, None, None
+        self._stop = threading.Event()
+        self.t = None
+
+    def __enter__(self):
+        import ctypes as C
+
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return self
+            dev = C.c_void_p()
+            # the CUDA device itself (NVML may number the GPUs differently), else the same index
+            if not (self.uuid and lib.nvmlDeviceGetHandleByUUID(self.uuid.encode(), C.byref(dev)) == 0) and \
+                    lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(dev)) != 0:
+                lib.nvmlShutdown()
+                return self
+            mx = C.c_uint(0)
+            if lib.nvmlDeviceGetMaxClockInfo(dev, C.c_int(1), C.byref(mx)) == 0:  # NVML_CLOCK_SM
+                self.max_mhz = float(mx.value)
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.lib, self.dev = lib, dev
+        except (OSError, AttributeError):
+            return self
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def _run(self):
+        import ctypes as C
+
+        clk, rs = C.c_uint(0), C.c_ulonglong(0)
+        while not self._stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.dev, C.c_int(1), C.byref(clk)) == 0 and \
+                    self.reasons_fn(self.dev, C.byref(rs)) == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            time.sleep(self.period)
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self.t is not None:
+            self.t.join(timeout=5)
+        if self.lib is not None:
+            self.lib.nvmlShutdown()
+
+    def summary(self):
+        if not self.samples:
+            return None
+        reasons = sorted({name for _, r in self.samples for bit, name in self.REASONS.items() if r & bit})
+        return {"sm_mhz": statistics.median(s for s, _ in self.samples), "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(self.samples), "source": "NVML, every ~1 ms during the timed region"}
+
+
 def issue_rate(warp_inst, kernel_ms, sm_mhz, n_sm):
     """Issue utilisation of an issue-bound kernel: warp instructions per launch (ncu
     smsp__inst_executed.sum) over the launch's CUDA-event duration, against the SM's ceiling of 4
@@ -539,7 +605,7 @@ def main():
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     total_ms = 0.0
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk, NvmlPoller(local, str(getattr(torch.cuda.get_device_properties(dev), "uuid", "") or "")) as nv:
         for _ in range(args.steps):
             flush.fill_(1.0)
             barrier()
@@ -620,7 +686,11 @@ def main():
         traffic, issue = pj.get("dram_bytes_per_launch"), pj.get("issue_active_pct")
         inst = {k: v.get("warp_instructions") for k, v in pj.get("per_kernel", {}).items()}
         l2 = pj.get("l2_bytes_per_launch")
-    clocks = clk.summary()
+    clocks = nv.summary()
+    if clocks is None:
+        clocks = clk.summary()
+    else:
+        clocks["nvidia_smi"] = clk.summary()
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
     k_each = {"k_fast_valid": k_ms / max(k_n, 1), "k_hard_queries": h_ms / max(h_n, 1)}
     issue_each = {k: issue_rate(inst.get(k), k_each[k], clocks["sm_mhz"], n_sm) for k in k_each}

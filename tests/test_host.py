@@ -474,3 +474,25 @@ def test_bench_cpu_baseline_rows():
     assert cb["value"] > 0 and cb["cores"] >= 1 and cb["kind"] == "port"
     assert cb["single_core"]["value"] > 0 and cb["single_core"]["cores"] == 1
     assert cb["value"] >= 0.5 * cb["single_core"]["value"]
+
+
+def test_bench_nvml_poller():
+    """bench.py's NVML clock poller: without NVML (or a GPU) it yields no summary, so the
+    nvidia-smi sampler's stands; its summary decodes the clock-event reason bits."""
+    import sys
+    import time
+
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    with bench.NvmlPoller(0, "0000-fake-uuid") as nv:
+        time.sleep(0.02)
+    s = nv.summary()
+    assert s is None or (s["samples"] > 0 and s["sm_mhz"] > 0)
+    p = bench.NvmlPoller(0)
+    p.samples = [(2070.0, 0x0), (2070.0, 0x4), (1995.0, 0x4 | 0x40), (2070.0, 0x1)]
+    p.max_mhz = 2070.0
+    s = p.summary()
+    assert s["sm_mhz"] == 2070.0 and s["samples"] == 4
+    assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+    assert bench.NvmlPoller(0, "abc").uuid == "GPU-abc" and bench.NvmlPoller(0, "GPU-abc").uuid == "GPU-abc"
