@@ -1,4 +1,5 @@
-"""Source rules of the CUDA kernels, checked on the text (no GPU, no compiler).
+"""Source rules, checked on the text (no GPU, no compiler): warp intrinsics in the CUDA kernels, and
+the commands the profile summaries give.
 
 A warp intrinsic with a full member mask (`__shfl_sync(0xffffffff, ...)`, `__any_sync`,
 `__ballot_sync`, ...) must be executed by every non-exited lane the mask names, at the same call.
@@ -64,3 +65,32 @@ def test_warp_intrinsics_are_unconditional(path):
     assert not bad, f"{path.name}: warp intrinsic evaluated conditionally at " + "; ".join(
         f"line {ln}: ...{ctx}" for ln, ctx in bad
     )
+
+
+def test_profile_commands_run_committed_files():
+    """Every profiles/ summary gives the command that made it, and that command runs committed
+    files: the scripts and modules it names exist here, and profile_cases knows the case it asks for."""
+    import re
+    import subprocess
+
+    repo = CSRC.parent.parent
+    tracked = set(subprocess.run(["git", "ls-files"], cwd=repo, capture_output=True, text=True).stdout.split())
+    if not tracked:
+        pytest.skip("not a git checkout")
+    cases = set(re.findall(r'which in \(([^)]*)\)', (repo / "plainmp_gb300" / "profile_cases.py").read_text()))
+    known = {c.strip().strip('"') for group in cases for c in group.split(",") if c.strip()}
+    summaries = sorted((repo / "profiles").glob("*.md"))
+    assert summaries
+    for md in summaries:
+        text = md.read_text()
+        cmds = re.findall(r"python3? (-m [\w.]+(?: \w+)?|[\w./]+\.py)", text)
+        assert cmds, f"{md.name} gives no command"
+        for c in cmds:
+            if c.startswith("-m "):
+                parts = c[3:].split()
+                path = parts[0].replace(".", "/") + ".py"
+                assert path in tracked, (md.name, c)
+                if parts[0].endswith("profile_cases") and len(parts) > 1:
+                    assert parts[1] in known, (md.name, c)
+            else:
+                assert c in tracked, (md.name, c)
