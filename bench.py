@@ -456,6 +456,28 @@ def bench_ik(dev, timed, steps=50, lr=0.05, fp32_peak=None):
     return out
 
 
+def traj_cost_check(cst, q32, off, margin=0.03, n=16):
+    """Relative error of the FP32 trajectory costs against the same cost in FP64, on the first n
+    trajectories, at the FP32 waypoints the kernel sees: the acceleration smoothing term on the
+    host, the hinge from the library's plain device method (exact FP64 per-sphere SDF distances,
+    sin/cos FK).  Error per trajectory: |c - c64| / max(1, |c64|)."""
+    from plainmp_gb300 import diff
+
+    if cst.groups()["only_self"].any():  # the hinge would need the active-sphere mask
+        return None
+    c32 = diff.traj_cost_grad(cst, q32[:off[n]], off[:n + 1], want_grad=False)
+    q = q32.astype(np.float64)
+    errs = []
+    for i in range(n):
+        P = q[off[i]:off[i + 1]]
+        d = np.asarray(cst.sphere_distances(P, high_accuracy=True))
+        acc = P[2:] - 2.0 * P[1:-1] + P[:-2]
+        ref = float((np.maximum(margin - d, 0.0) ** 2).sum() + (acc ** 2).sum())
+        errs.append(abs(float(c32[i]) - ref) / max(1.0, abs(ref)))
+    return {"trajectories": n, "max_rel_err": max(errs),
+            "reference": "the same cost in FP64: smoothing on the host, hinge from the plain method's FP64 distances"}
+
+
 def bench_traj(dev, timed):
     """C4: 512 trajectories (20-100 waypoints) of the planar-base chain (x, y, yaw + 7 joints)
     against the 200k-point cloud; one eval = cost + gradient of one trajectory (FK recomputed
@@ -502,6 +524,10 @@ def bench_traj(dev, timed):
     }
     if err:
         out["autograd_cuda_graph_error"] = err
+    try:
+        out["fp64_check"] = traj_cost_check(cst, Qh, off)
+    except Exception as e:  # noqa: BLE001  (reported in the line; the rates above stand)
+        out["fp64_check"] = {"error": f"{type(e).__name__}: {e}"}
     return out
 
 

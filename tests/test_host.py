@@ -496,3 +496,39 @@ def test_bench_nvml_poller():
     assert s["sm_mhz"] == 2070.0 and s["samples"] == 4
     assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
     assert bench.NvmlPoller(0, "abc").uuid == "GPU-abc" and bench.NvmlPoller(0, "GPU-abc").uuid == "GPU-abc"
+
+
+def test_bench_traj_cost_check(monkeypatch):
+    """bench.py's C4 FP64 check on stand-ins for the device calls: the reference is the smoothing
+    term plus the hinge of the FP64 distances, per trajectory, and the reported error is relative."""
+    import sys
+
+    sys.path.insert(0, str(REPO))
+    import bench
+    from plainmp_gb300 import diff
+    from plainmp_gb300 import workloads as W
+
+    trajs = W.trajectories(20, seed=3)
+    q32 = np.concatenate(trajs, axis=0).astype(np.float32)
+    off = np.concatenate([[0], np.cumsum([len(t) for t in trajs])]).astype(np.int64)
+
+    class FakeCst:
+        def groups(self):
+            return {"only_self": np.zeros(3, bool)}
+
+        def sphere_distances(self, P, high_accuracy=False):
+            return np.full((len(P), 4), 0.01) + 0.001 * np.arange(4)  # every sphere inside the 0.03 margin
+
+    def fake_cost(cst, q, o, want_grad=True):
+        P = q.astype(np.float64)
+        out = []
+        for i in range(len(o) - 1):
+            T = P[o[i]:o[i + 1]]
+            acc = T[2:] - 2 * T[1:-1] + T[:-2]
+            d = cst.sphere_distances(T)
+            out.append((acc ** 2).sum() + (np.maximum(0.03 - d, 0) ** 2).sum())
+        return np.asarray(out, np.float32)
+
+    monkeypatch.setattr(diff, "traj_cost_grad", fake_cost)
+    r = bench.traj_cost_check(FakeCst(), q32, off)
+    assert r["trajectories"] == 16 and 0 <= r["max_rel_err"] < 1e-6  # FP32 rounding of the cost only
