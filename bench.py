@@ -41,8 +41,22 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 B = 65536
 
 
+def _workloads():
+    """The seeded generators (plainmp_gb300/workloads.py), loaded by file path: importing the
+    package would load the product library, which the CPU arms must not touch."""
+    import importlib.util
+
+    name = "_pm_workloads"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, ROOT / "plainmp_gb300" / "workloads.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
 def workload():
-    from plainmp_gb300 import workloads as W
+    W = _workloads()
 
     robot = W.dualarm_robot()
     scene = W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0)
@@ -201,14 +215,29 @@ def peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def cpu_baseline(robot, scene, q, seconds: float = 6.0):
-    """The oracle (CPU FP64 restatement of the reference's is_valid loop) on all host cores,
-    over a bounded sample of the batch: validity only, as the reference computes it."""
-    from oracle import pyoracle
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform string)."""
+    import platform
 
-    threads = os.cpu_count() or 1
-    _, oc, _ = pyoracle.make_constraint(robot, scene)
-    n = 4096
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for ln in r.stdout.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip() + f" ({platform.machine()})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def _oracle_rate(oc, q, threads: int, n: int, seconds: float):
+    """configs/s of the oracle's is_valid loop over slices of n configurations of q, repeated for
+    about `seconds`: (rate, configurations done, repetitions)."""
     t0 = time.perf_counter()
     oc.is_valid(q[:n], threads=threads)
     dt = time.perf_counter() - t0
@@ -216,24 +245,49 @@ def cpu_baseline(robot, scene, q, seconds: float = 6.0):
     done = 0
     t0 = time.perf_counter()
     for r in range(reps):
-        off = (r * n) % (B - n)
+        off = (r * n) % max(len(q) - n, 1)
         oc.is_valid(q[off:off + n], threads=threads)
         done += n
-    dt = time.perf_counter() - t0
-    out = {"value": done / dt, "unit": "configs/s", "cores": threads, "kind": "port",
-           "sample": f"{done} configs of the same batch ({reps} x {n}), validity only (the reference has no per-sphere distance output)"}
+    return done / (time.perf_counter() - t0), done, reps
+
+
+def cpu_row(seconds: float = 4.0) -> dict:
+    """All-core oracle rate on the headline batch in this process (PM_ORACLE_CONTRACT selects the
+    build); run by cpu_baseline in a child process for the contraction-on build."""
+    from oracle import pyoracle
+
+    robot, scene, q = workload()
+    threads = os.cpu_count() or 1
+    _, oc, _ = pyoracle.make_constraint(robot, scene)
+    rate, done, reps = _oracle_rate(oc, q, threads, 4096, seconds)
+    return {"value": rate, "unit": "configs/s", "cores": threads, "sample": f"{done} configs ({reps} x 4096)",
+            "build": "-O3 -ffp-contract=fast" if pyoracle.CONTRACT else "-O3 -ffp-contract=off"}
+
+
+def cpu_baseline(robot, scene, q, seconds: float = 6.0):
+    """The oracle (CPU FP64 restatement of the reference's is_valid loop) on all host cores,
+    over a bounded sample of the batch: validity only, as the reference computes it.  Rows: the
+    bit-exact build (-ffp-contract=off, the headline figure), one core of it, and the build with
+    contraction on (-ffp-contract=fast, timed in a child process)."""
+    from oracle import pyoracle
+
+    threads = os.cpu_count() or 1
+    _, oc, _ = pyoracle.make_constraint(robot, scene)
+    rate, done, reps = _oracle_rate(oc, q, threads, 4096, seconds)
+    out = {"value": rate, "unit": "configs/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+           "build": "-O3 -ffp-contract=off",
+           "sample": f"{done} configs of the same batch ({reps} x 4096), validity only (the reference has no per-sphere distance output)"}
     # one core, as one planner process runs the reference's is_valid loop
-    n1 = 1024
-    t0 = time.perf_counter()
-    oc.is_valid(q[:n1], threads=1)
-    dt = time.perf_counter() - t0
-    reps = max(1, min(32, int(seconds / 3 / max(dt, 1e-6))))
-    t0 = time.perf_counter()
-    for r in range(reps):
-        off = (r * n1) % (B - n1)
-        oc.is_valid(q[off:off + n1], threads=1)
-    dt = time.perf_counter() - t0
-    out["single_core"] = {"value": reps * n1 / dt, "unit": "configs/s", "cores": 1, "sample": f"{reps * n1} configs ({reps} x {n1})"}
+    r1, done1, reps1 = _oracle_rate(oc, q, 1, 1024, seconds / 3)
+    out["single_core"] = {"value": r1, "unit": "configs/s", "cores": 1, "sample": f"{done1} configs ({reps1} x 1024)"}
+    try:
+        env = dict(os.environ, PM_ORACLE_CONTRACT="1")
+        r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--cpu-row"], capture_output=True, text=True, env=env,
+                           timeout=600)
+        out["contract_build"] = json.loads(r.stdout.strip().splitlines()[-1]) if r.returncode == 0 else \
+            {"error": (r.stderr.strip().splitlines() or ["failed"])[-1]}
+    except (OSError, subprocess.SubprocessError, ValueError, IndexError) as e:
+        out["contract_build"] = {"error": f"{type(e).__name__}: {e}"}
     return out
 
 
@@ -532,6 +586,10 @@ def bench_traj(dev, timed):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's is_valid loop (kind "port"; the
+    reference itself does not build here) on all host cores, over the whole 65,536-configuration
+    batch per step.  It loads the oracle alone: the seeded generators come by file path, so the
+    product library stays out of this process."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -540,24 +598,24 @@ def run_reference(args):
 
     threads = os.cpu_count() or 1
     _, oc, _ = pyoracle.make_constraint(robot, scene)
-    n = 8192
     for w in range(args.warmup):
-        oc.is_valid(q[:n], threads=threads)
+        oc.is_valid(q, threads=threads)
     times = []
     for k in range(args.steps):
-        off = (k * n) % (B - n)
         t0 = time.perf_counter()
-        oc.is_valid(q[off:off + n], threads=threads)
+        oc.is_valid(q, threads=threads)
         times.append(time.perf_counter() - t0)
     total = sum(times)
-    value = n * args.steps / total
+    value = B * args.steps / total
     line = {
         "impl": "reference", "metric": "configs checked/sec", "value": value, "unit": "configs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": config_dict({"reference_sample_per_step": n}),
-        "cpu_baseline": {"value": value, "unit": "configs/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} configs per step of the same batch, validity only"},
+        "config": config_dict({"l2": "not applicable (CPU)"}),
+        "cpu_baseline": {"value": value, "unit": "configs/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+                         "build": "-O3 -ffp-contract=off",
+                         "sample": f"the whole {B}-configuration batch per step, validity only (the reference has no "
+                                   "per-sphere distance output)"},
         "e2e": {"value": value, "unit": "configs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -571,7 +629,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true", help="skip the C0/C1/C3/C4 side measurements")
+    ap.add_argument("--cpu-row", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.cpu_row:
+        print(json.dumps(cpu_row()), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -196,7 +196,8 @@ int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* t
  * with PMGPU_MEM_DEVICE: q, out and dist32 (optional) are device pointers and the work is
  * enqueued on `stream`.  Its scratch is a fixed file-scope device array of about 2 MB (held on
  * every device that loads the library until exit); the first call on a device looks up that
- * array's address, so make it before any stream capture.  Requirements and limits: B <= 1048576
+ * array's address and uploads a small search table (a synchronous copy, unless an allocating
+ * fast call did it before), so make it before any stream capture.  Requirements and limits: B <= 1048576
  * (larger batches return PMGPU_ERR_INVALID); the constraint's tables must already be on the
  * device from an earlier batch call (else PMGPU_ERR_RUNTIME, never an allocation); calls that
  * overlap on the GPU share the scratch array and race.  Error text: pmgpu_last_error(). */

@@ -19,23 +19,28 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
-LIB = BUILD / "liboracle.so"
+# PM_ORACLE_CONTRACT=1 selects a second build with floating-point contraction on
+# (-ffp-contract=fast: FMA where the compiler finds one, the GNU dialects' default).  Its results
+# may differ from the restatement's in the last bits; it exists only as a CPU timing row.
+CONTRACT = os.environ.get("PM_ORACLE_CONTRACT", "") == "1"
+LIB = BUILD / ("liboracle_contract.so" if CONTRACT else "liboracle.so")
 
 _TYPES = {"revolute": 1, "continuous": 2, "prismatic": 3, "floating": 4, "planar": 5, "fixed": 6}
 
 
-def build(force: bool = False) -> Path:
-    """Compile the oracle (g++, -O3 -ffp-contract=off)."""
+def build(force: bool = False, contract: bool = CONTRACT) -> Path:
+    """Compile the oracle (g++, -O3 -ffp-contract=off; with contract, -ffp-contract=fast)."""
     BUILD.mkdir(exist_ok=True)
     src = HERE / "oracle.cpp"
-    if LIB.exists() and not force and LIB.stat().st_mtime > src.stat().st_mtime:
-        return LIB
-    tmp = BUILD / f"liboracle.{os.getpid()}.so"
-    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", str(src),
-           "-o", str(tmp)]
+    lib_path = BUILD / ("liboracle_contract.so" if contract else "liboracle.so")
+    if lib_path.exists() and not force and lib_path.stat().st_mtime > src.stat().st_mtime:
+        return lib_path
+    tmp = BUILD / f"{lib_path.stem}.{os.getpid()}.so"
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O3", "-ffp-contract=fast" if contract else "-ffp-contract=off", "-fPIC",
+           "-shared", "-pthread", str(src), "-o", str(tmp)]
     subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 _lib = None

@@ -2,9 +2,11 @@
 # Test infrastructure only.  Compiles the reference's vendored URDF parser (urdfdom + tinyxml,
 # third/urdf_parser under the reference checkout) with oracle/ref/urdf_dump.cpp into
 # oracle/_ref/urdf_dump.  Reads the sources where they lie; writes only into oracle/_ref/.
-# Usage: oracle/ref/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/ref/build_ref.sh [reference_root]
+#   reference_root: the argument, else $PLAINMP_REF, else the checkout's location in the build
+#   container (/root/reference).  Exits 1 without building when the parser sources are absent.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${PLAINMP_REF:-/root/reference}}
 U="$REF/third/urdf_parser"
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"

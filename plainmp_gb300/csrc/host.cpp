@@ -1818,6 +1818,8 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     check_arr(q, B * C.q_dim(), "q");
     check_arr(out, B, "out");
     const PmTablesHdr* T = C.tables();
+    if (!fast_table_sizes_ok(C.hdr))
+      fail(PMGPU_ERR_INVALID, "is_valid_fast: at most 65535 spheres and 32767 primitives (use is_valid_batch)");
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
     if (mem == PMGPU_MEM_HOST && B >= 16384) {
@@ -1925,6 +1927,8 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
     check_arr(s2, E * C.q_dim(), "s2");
     check_arr(out, E, "out");
     const PmTablesHdr* T = C.tables();
+    if (!fast_table_sizes_ok(C.hdr))
+      fail(PMGPU_ERR_INVALID, "check_motion_fast: at most 65535 spheres and 32767 primitives (use check_motion_batch)");
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
     const int16_t* seq = C.seq_table();
@@ -1957,12 +1961,8 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
       d2 = stage_in(C.w_in2, s2, (size_t)E * d, s);
       dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)E, 16));
     }
-    static int n_sm = 0;
-    if (n_sm == 0) {
-      int dev = 0;
-      cuda_check(cudaGetDevice(&dev), "device");
-      cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
-    }
+    int n_sm = 0;
+    cuda_check(sm_count(&n_sm), "device attribute");
     cuda_check(launch_fast_edges(T, C.hdr, st, d1, d2, E, validator_type, dw, resolution, seq, sr, n, off, next, dout, items, count, cap,
                                  ovf, dstats, 32, n_sm, s),
                "check_motion_fast");

@@ -22,6 +22,7 @@
 // also fails, so certain terms need no FP64 work.  Self pairs factor the same way.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "pm_grad.cuh"
@@ -1448,9 +1449,46 @@ namespace pmg {
 
 size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist) { return smem_layout(h, cpb, want_dist).total; }
 
-static cudaError_t upload_offsets() {
-  static bool done = false;
-  if (done) return cudaSuccess;
+// Queue records pack a sphere index in 16 bits and a primitive index in 15 (HardQuery.b.y: sphere |
+// primitive << 16 | check << 31; the block's queue: configuration << 16 | sphere).  The tables of
+// such sizes would not fit in shared memory anyway; the launchers refuse them explicitly.
+bool fast_table_sizes_ok(const PmTablesHdr& h) { return h.n_spheres <= 0xffff && h.n_prims <= 0x7fff; }
+
+// Per-device state of this file's kernels: __device__ symbols (the offset table below) exist once
+// per device, so each device gets its own upload, and SM counts may differ between devices.
+constexpr int kMaxDev = 64;
+static std::mutex g_dev_mu;
+static bool g_off_done[kMaxDev];
+static int g_sm_count[kMaxDev];
+
+static cudaError_t current_device(int* dev) {
+  cudaError_t e = cudaGetDevice(dev);
+  if (e == cudaSuccess && (*dev < 0 || *dev >= kMaxDev)) e = cudaErrorInvalidDevice;
+  return e;
+}
+
+// Number of SMs of the current device (cached per device).
+cudaError_t sm_count(int* n) {
+  int dev = 0;
+  cudaError_t e = current_device(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (g_sm_count[dev] <= 0) {
+    int v = 0;
+    if ((e = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    g_sm_count[dev] = v > 0 ? v : 1;
+  }
+  *n = g_sm_count[dev];
+  return cudaSuccess;
+}
+
+// Uploads the sorted block offsets (c_off, c_off_lb) to the current device, once per device.
+cudaError_t upload_offsets() {
+  int dev = 0;
+  cudaError_t e = current_device(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (g_off_done[dev]) return cudaSuccess;
   std::vector<std::pair<float, char4>> v;
   for (int z = -kOffR; z <= kOffR; z++)
     for (int y = -kOffR; y <= kOffR; y++)
@@ -1472,9 +1510,9 @@ static cudaError_t upload_offsets() {
     off[i] = v[i].second;
     lb[i] = v[i].first;
   }
-  cudaError_t e = cudaMemcpyToSymbol(c_off, off.data(), off.size() * sizeof(char4));
+  e = cudaMemcpyToSymbol(c_off, off.data(), off.size() * sizeof(char4));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_off_lb, lb.data(), lb.size() * sizeof(float));
-  if (e == cudaSuccess) done = true;
+  if (e == cudaSuccess) g_off_done[dev] = true;
   return e;
 }
 
@@ -1491,6 +1529,7 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq,
                               unsigned long long* hq_count, unsigned int hq_cap) {
   if (B <= 0) return cudaSuccess;
+  if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   // (hard-query entries hold 32-bit configuration indices)
   const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
@@ -1520,17 +1559,16 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_end("k_fast_valid", s);
   CfgSource src{q, B, out};
+  int n_sm = 0;
+  if ((e = sm_count(&n_sm)) != cudaSuccess) return e;
   if (split) {
-    int dev = 0, n_sm = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     prof_begin("k_hard_queries", s);
     k_hard_queries<CfgSource><<<n_sm * 4, 256, 0, s>>>(T, scr.hq, dist32, src, scr);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_end("k_hard_queries", s);
   }
   prof_begin("k_fast_recheck", s);
-  k_fast_recheck<CfgSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
+  k_fast_recheck<CfgSource><<<n_sm * 4, 128, 0, s>>>(T, state, src, scr);
   prof_end("k_fast_recheck", s);
   return cudaGetLastError();
 }
@@ -1542,6 +1580,7 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
                               int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
                               unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int n_sm, cudaStream_t s) {
   if (E <= 0) return cudaSuccess;
+  if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   Scratch scr{items, count, cap, overflow, stats};
   k_edge_setup<<<(unsigned)((E + 127) / 128), 128, 0, s>>>(s1, s2, E, h.q_dim, type, width, resolution, sr, n, out);
   cudaError_t e = cudaGetLastError();
@@ -1560,7 +1599,7 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   prof_end("k_fast_edges", s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_begin("k_fast_recheck_edges", s);
-  k_fast_recheck<EdgeSource><<<152 * 4, 128, 0, s>>>(T, state, src, scr);
+  k_fast_recheck<EdgeSource><<<n_sm * 4, 128, 0, s>>>(T, state, src, scr);
   prof_end("k_fast_recheck_edges", s);
   return cudaGetLastError();
 }

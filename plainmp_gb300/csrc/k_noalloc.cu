@@ -12,7 +12,10 @@
 // the library holds a copy until the process exits.  Host code must not pass the symbol itself
 // to a kernel (it names a host-side stand-in); the device address comes from
 // cudaGetSymbolAddress, taken once per device, with that device current, on the first call made
-// on it -- so make that first call before any stream capture.  All calls share the array and it
+// on it.  That first call also uploads the warp search's block-offset table to the device (a
+// synchronous cudaMemcpyToSymbol, unless an allocating fast call did it before) -- so make that
+// first call before any stream capture and outside any section that must not block.  All calls
+// share the array and it
 // keeps the last call's contents: the counters and flags are cleared (cudaMemsetAsync) at the
 // start of every call, and calls that overlap on the GPU (two streams, or two constraints at
 // once) race on it.
@@ -75,6 +78,11 @@ extern "C" int pmgpu_cst_is_valid_fast_noalloc(pmgpu_cst* c, const double* q, in
       if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(PMGPU_ERR_CUDA, cudaGetErrorString(e));
+      }
+      const cudaError_t eo = pmg::upload_offsets();  // once per device too; later calls find it done
+      if (eo != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PMGPU_ERR_CUDA, cudaGetErrorString(eo));
       }
       g_addr[dev] = static_cast<unsigned char*>(p);
     }

@@ -39,6 +39,12 @@ cudaError_t launch_check_motion64(const PmTablesHdr* T, const double* state, con
 
 // ---- fast path (k_fast.cu): FP32 decisions + FP64 recheck of uncertain terms.
 size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist);
+// The fast kernels' queue records hold at most 65,535 spheres and 32,767 primitives.
+bool fast_table_sizes_ok(const PmTablesHdr& h);
+// SM count of the current device (cached per device); the offset table of the warp searches,
+// uploaded to the current device once.
+cudaError_t sm_count(int* n);
+cudaError_t upload_offsets();
 // hq (hq_cap 32-byte entries) and hq_count (zeroed by the caller): with distances, the hard cloud
 // queries are answered by a second kernel over this global queue; null keeps them in the block.
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import importlib.util
 import json
+import os
 import subprocess
 import sys
 import tempfile
@@ -94,7 +95,10 @@ def urdf_fixture(name: str, urdf: str, dump: Path) -> None:
 
 
 def main() -> None:
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PLAINMP_REF")
+    if not arg:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set PLAINMP_REF to the plainmp checkout)")
+    ref = Path(arg)
     sequence_table(ref)
     subprocess.run([str(REPO / "oracle/ref/build_ref.sh"), str(ref)], check=True)
     dump = REPO / "oracle/_ref/urdf_dump"

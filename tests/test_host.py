@@ -271,6 +271,25 @@ def test_bench_reference_arm_line():
     assert d["value"] > 0 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert str(d["config"]["batch_configs"]) in d["cpu_baseline"]["sample"]  # the whole batch, every step
+
+
+def test_bench_reference_arm_loads_no_product_library():
+    """The reference arm runs the oracle alone: neither the product package nor its library is
+    loaded into its process (the seeded generators come by file path)."""
+    import subprocess
+    import sys
+
+    code = ("import argparse, sys; sys.path.insert(0, %r); import bench; "
+            "bench.run_reference(argparse.Namespace(steps=1, warmup=0, gpus=1)); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'libpmgpu' not in maps, 'product library loaded'; "
+            "assert 'liboracle' in maps; "
+            "assert not any(m == 'plainmp_gb300' or m.startswith('plainmp_gb300.') for m in sys.modules), 'package imported'; "
+            "print('clean')") % str(REPO)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=str(REPO))
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().endswith("clean")
 
 
 def test_output_buffers_are_validated():
@@ -474,6 +493,11 @@ def test_bench_cpu_baseline_rows():
     assert cb["value"] > 0 and cb["cores"] >= 1 and cb["kind"] == "port"
     assert cb["single_core"]["value"] > 0 and cb["single_core"]["cores"] == 1
     assert cb["value"] >= 0.5 * cb["single_core"]["value"]
+    assert isinstance(cb["cpu_model"], str) and cb["cpu_model"]
+    assert cb["build"] == "-O3 -ffp-contract=off"
+    cc = cb["contract_build"]  # the second build, contraction on, timed in a child process
+    assert cc.get("value", 0) > 0, cc
+    assert cc["build"] == "-O3 -ffp-contract=fast" and cc["cores"] == cb["cores"]
 
 
 def test_bench_nvml_poller():

@@ -99,6 +99,31 @@ def test_evaluate_and_is_valid_mobile_base(oracle, base):
     assert (got != ref).sum() == 0
 
 
+def test_evaluate_dualarm_cloud(dual):
+    """evaluate() against the point cloud: the ext row's value is the clamped minimum over spheres
+    of the cloud distance (exact nearest point, KD-tree in the oracle) and its Jacobian row the
+    forward-difference SDF gradient of the argmin sphere through the attached-point Jacobian
+    (primitive_sphere_collision.cpp:256-322, primitive_sdf.hpp:597-603).  Values within 1e-9 on
+    every configuration; Jacobian rows within 1e-9 where the argmin sphere is unambiguous (the two
+    smallest sphere distances at least 1e-6 apart: a tie may pick either sphere)."""
+    import os
+
+    (_, cst, _), (_, oc, _) = dual
+    assert not cst.groups()["only_self"].any()  # every sphere takes part in the ext row
+    Q = W.dualarm_configs(2048, seed=21)
+    v, J = cst.evaluate_batch(Q)
+    rv, rJ = oc.evaluate(Q, threads=os.cpu_count() or 8)
+    assert v.shape == (2048, 2) and J.shape == (2048, 2, 14)
+    np.testing.assert_allclose(v, rv, atol=1e-9, rtol=0)
+    d = np.sort(oc.sphere_distances(Q, threads=os.cpu_count() or 8), axis=1)
+    near = d[:, 0] < 0.1  # the row is active (below the cutoff): its Jacobian is not zero
+    clear = (d[:, 1] - d[:, 0]) > 1e-6
+    assert near.sum() > 100 and (near & clear).sum() > 0.9 * near.sum()
+    np.testing.assert_allclose(J[clear, 0], rJ[clear, 0], atol=1e-9, rtol=0)
+    np.testing.assert_allclose(J[:, 1], rJ[:, 1], atol=1e-9, rtol=0)  # self row: no SDF involved
+    assert np.array_equal(cst.is_valid_batch(Q), oc.is_valid(Q, threads=os.cpu_count() or 8))
+
+
 def test_evaluate_empty_and_self_only(oracle):
     (_, cst, _), (_, oc, _) = both(oracle, W.chain7_robot(), None, self_collision=False)
     Q = W.chain7_configs(17)
