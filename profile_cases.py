@@ -2,10 +2,13 @@
 configurations against the 200k-point box-surface cloud, validity only (``valid``) or with the
 per-sphere distances (``dist``), three launches each; one fused IK descent (8192 problems x 50
 steps, ``ik``); one trajectory cost + gradient (512 trajectories, ``traj``).
-python -m plainmp_gb300.profile_cases [valid|dist|ik|traj|all]"""
+python profile_cases.py [valid|dist|ik|traj|all]"""
 import sys
+from pathlib import Path
 
 import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 
 def fast(distances: bool, n: int = 65536, launches: int = 3):

@@ -1,9 +1,13 @@
-"""The bindings shown in INTEGRATION.md, built from the document's own text.
+"""The bindings INTEGRATION.md shows, built from their committed sources
+(plainmp_gb300/bindings/).
 
-* The pybind11 binding compiles against include/pmgpu.h, links to the in-tree library and works.
-  Without a GPU its is_valid_batch reports the library's "no CUDA device" error; with one it equals
-  the Python mirror's plain method.  Needs pybind11 (skipped where it is absent).
-* The OMPL adapter compiles against include/pmgpu.h and a stand-in of the OMPL declarations it uses.
+* The pybind11 binding (pybind11_gpu_cst.cpp) compiles against include/pmgpu.h, links to the
+  in-tree library and works.  Without a GPU its is_valid_batch reports the library's "no CUDA
+  device" error; with one it equals the Python mirror's plain method.  Needs pybind11 (skipped
+  where it is absent).
+* The OMPL adapter (ompl_adapter.hpp) compiles against include/pmgpu.h and a stand-in of the OMPL
+  declarations it uses.
+* INTEGRATION.md quotes both files' code as it stands.
 * A C99 program includes the header, links to the library and calls it (the ABI is plain C).
 """
 import importlib.util
@@ -16,27 +20,26 @@ import numpy as np
 import pytest
 
 REPO = Path(__file__).resolve().parent.parent
+BINDINGS = REPO / "plainmp_gb300" / "bindings"
 
-HARNESS = """#include <pybind11/pybind11.h>
-#include <pybind11/numpy.h>
-#include <pybind11/stl.h>
-#include <memory>
-#include <stdexcept>
-#include <string>
-#include <tuple>
-#include <vector>
+MODULE = """#include <pybind11/pybind11.h>
 namespace py = pybind11;
-{snippet}
-PYBIND11_MODULE(gpu_stub, m) {{ bind_gpu_constraint(m); }}
+void bind_gpu_constraint(py::module& cst_m);
+PYBIND11_MODULE(gpu_stub, m) { bind_gpu_constraint(m); }
 """
 
 
-def pybind11_section() -> str:
-    """The C++ block of INTEGRATION.md's pybind11 section."""
+def doc_block(section: str) -> str:
+    """The C++ block of an INTEGRATION.md section."""
     text = (REPO / "INTEGRATION.md").read_text()
-    sec = text[text.index("## 4. pybind11"):]
+    sec = text[text.index(section):]
     start = sec.index("```cpp\n") + len("```cpp\n")
     return sec[start:sec.index("```", start)]
+
+
+def test_document_quotes_the_sources():
+    assert doc_block("## 3. C++ (OMPL") in (BINDINGS / "ompl_adapter.hpp").read_text()
+    assert doc_block("## 4. pybind11") in (BINDINGS / "pybind11_gpu_cst.cpp").read_text()
 
 
 @pytest.fixture(scope="module")
@@ -44,11 +47,12 @@ def stub(tmp_path_factory):
     pybind11 = pytest.importorskip("pybind11")
     d = tmp_path_factory.mktemp("stub")
     src = d / "gpu_stub.cpp"
-    src.write_text(HARNESS.format(snippet=pybind11_section()))
+    src.write_text(MODULE)
     so = d / ("gpu_stub" + sysconfig.get_config_var("EXT_SUFFIX"))
     lib_dir = REPO / "plainmp_gb300"
     cmd = ["g++", "-std=c++17", "-O0", "-shared", "-fPIC", "-Wall", f"-I{REPO / 'include'}", f"-I{pybind11.get_include()}",
-           f"-I{sysconfig.get_paths()['include']}", str(src), "-o", str(so), f"-L{lib_dir}", "-lpmgpu", f"-Wl,-rpath,{lib_dir}"]
+           f"-I{sysconfig.get_paths()['include']}", str(src), str(BINDINGS / "pybind11_gpu_cst.cpp"), "-o", str(so), f"-L{lib_dir}",
+           "-lpmgpu", f"-Wl,-rpath,{lib_dir}"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-3000:]
     spec = importlib.util.spec_from_file_location("gpu_stub", so)
@@ -76,23 +80,18 @@ def test_pybind11_stub_builds_and_runs(stub):
     assert np.array_equal(c.is_valid_batch(Q), mine.is_valid_batch(Q))
 
 
-# The OMPL declarations the adapter of INTEGRATION.md section 3 uses (OMPL itself is not installed):
+# Stand-ins of the OMPL headers the adapter includes (OMPL itself is not installed):
 # State::as<T>(), RealVectorStateSpace::StateType::values, MotionValidator's constructor and its two
 # pure checkMotion overloads, SpaceInformationPtr.
-OMPL_DECLS = """#include <memory>
-#include <stdexcept>
+OMPL_MOTION_VALIDATOR_H = """#pragma once
+#include <memory>
 #include <utility>
-#include <vector>
 namespace ompl { namespace base {
 class State {
  public:
   virtual ~State() = default;
   template <class T> const T* as() const { return static_cast<const T*>(this); }
   template <class T> T* as() { return static_cast<T*>(this); }
-};
-class RealVectorStateSpace {
- public:
-  class StateType : public State { public: double* values = nullptr; };
 };
 class SpaceInformation {};
 using SpaceInformationPtr = std::shared_ptr<SpaceInformation>;
@@ -107,19 +106,29 @@ class MotionValidator {
 };
 }}  // namespace ompl::base
 """
+OMPL_REAL_VECTOR_H = """#pragma once
+#include <ompl/base/MotionValidator.h>
+namespace ompl { namespace base {
+class RealVectorStateSpace {
+ public:
+  class StateType : public State { public: double* values = nullptr; };
+};
+}}  // namespace ompl::base
+"""
 
 
 def test_ompl_adapter_compiles(tmp_path):
-    """INTEGRATION.md's OMPL adapter compiles against include/pmgpu.h (its ABI calls have the
-    header's argument lists) and implements both checkMotion overloads."""
-    text = (REPO / "INTEGRATION.md").read_text()
-    sec = text[text.index("## 3. C++ (OMPL"):]
-    start = sec.index("```cpp\n") + len("```cpp\n")
+    """The OMPL adapter header compiles against include/pmgpu.h (its ABI calls have the header's
+    argument lists) and implements both checkMotion overloads."""
+    inc = tmp_path / "inc" / "ompl" / "base"
+    (inc / "spaces").mkdir(parents=True)
+    (inc / "MotionValidator.h").write_text(OMPL_MOTION_VALIDATOR_H)
+    (inc / "spaces" / "RealVectorStateSpace.h").write_text(OMPL_REAL_VECTOR_H)
     src = tmp_path / "adapter.cpp"
-    src.write_text(OMPL_DECLS + sec[start:sec.index("```", start)] +
-                   "\nint main() { GpuBoxMotionValidator v(nullptr, nullptr, {0.05}); (void)v; return 0; }\n")
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", f"-I{REPO / 'include'}", str(src)],
-                       capture_output=True, text=True, timeout=120)
+    src.write_text('#include "ompl_adapter.hpp"\n'
+                   "int main() { GpuBoxMotionValidator v(nullptr, nullptr, {0.05}); GpuValidity g{nullptr, 7}; (void)v; (void)g; return 0; }\n")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", f"-I{tmp_path / 'inc'}", f"-I{BINDINGS}",
+                        f"-I{REPO / 'include'}", str(src)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr[-3000:]
 
 

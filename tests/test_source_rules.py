@@ -77,20 +77,21 @@ def test_profile_commands_run_committed_files():
     tracked = set(subprocess.run(["git", "ls-files"], cwd=repo, capture_output=True, text=True).stdout.split())
     if not tracked:
         pytest.skip("not a git checkout")
-    cases = set(re.findall(r'which in \(([^)]*)\)', (repo / "plainmp_gb300" / "profile_cases.py").read_text()))
+    cases = set(re.findall(r'which in \(([^)]*)\)', (repo / "profile_cases.py").read_text()))
     known = {c.strip().strip('"') for group in cases for c in group.split(",") if c.strip()}
     summaries = sorted((repo / "profiles").glob("*.md"))
     assert summaries
     for md in summaries:
         text = md.read_text()
-        cmds = re.findall(r"python3? (-m [\w.]+(?: \w+)?|[\w./]+\.py)", text)
+        cmds = re.findall(r"python3? (-m [\w.]+(?: \w+)?|[\w./]+\.py(?: \w+)?)", text)
         assert cmds, f"{md.name} gives no command"
         for c in cmds:
             if c.startswith("-m "):
                 parts = c[3:].split()
                 path = parts[0].replace(".", "/") + ".py"
                 assert path in tracked, (md.name, c)
-                if parts[0].endswith("profile_cases") and len(parts) > 1:
-                    assert parts[1] in known, (md.name, c)
             else:
-                assert c in tracked, (md.name, c)
+                parts = c.split()
+                assert parts[0] in tracked, (md.name, c)
+                if parts[0] == "profile_cases.py" and len(parts) > 1:
+                    assert parts[1] in known, (md.name, c)
