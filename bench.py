@@ -585,6 +585,123 @@ def bench_traj(dev, timed):
     return out
 
 
+def bench_single_calls(n: int = 2000):
+    """Per-call latency of the calls OMPL's callbacks make, one state or one edge at a time, through
+    the C ABI with host memory: the state-validity hook calls is_valid per state
+    (ompl_thin_wrap.hpp:114-120), the motion validator checkMotion per edge (motion_validator.cpp:
+    17-79).  Beside each, the oracle's single-core time per state or edge (its own C loop over the
+    same inputs, no binding in between).  The library's figures go through ctypes (about 1 us of
+    binding per call)."""
+    import ctypes as C
+
+    from oracle import pyoracle
+    from plainmp_gb300 import _lib, scenes
+
+    W = _workloads()
+    lib = _lib.lib
+    out = {}
+    cases = [("C0", W.chain7_robot(), W.chain7_scene(), W.chain7_configs(n, seed=41)),
+             ("C2", W.dualarm_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0), W.dualarm_configs(n, seed=42))]
+    for name, robot, scene, qs in cases:
+        _, cst, _ = scenes.make_constraint(robot, scene)
+        _, oc, _ = pyoracle.make_constraint(robot, scene)
+        qs = np.ascontiguousarray(qs)
+        ok = np.zeros(1, np.uint8)
+        optr = C.c_void_p(ok.ctypes.data)
+        ptrs = [C.c_void_p(qs[i].ctypes.data) for i in range(n)]
+        got = np.empty(n, np.uint8)
+        for i in range(min(n, 50)):  # warm-up (tables, staging buffers)
+            lib.pmgpu_cst_is_valid(cst._h, ptrs[i], 1, optr, _lib.MEM_HOST, None)
+        t0 = time.perf_counter()
+        for i in range(n):
+            if lib.pmgpu_cst_is_valid(cst._h, ptrs[i], 1, optr, _lib.MEM_HOST, None) != 0:
+                raise RuntimeError(lib.pmgpu_last_error().decode())
+            got[i] = ok[0]
+        gpu_us = (time.perf_counter() - t0) / n * 1e6
+        t0 = time.perf_counter()
+        ref = oc.is_valid(qs, threads=1)
+        cpu_us = (time.perf_counter() - t0) / n * 1e6
+        out[name] = {"is_valid_per_call_us": gpu_us, "oracle_single_core_us": cpu_us, "identical": bool(np.array_equal(got, ref)),
+                     "calls": n}
+    # one edge at a time: checkMotion of the box validator (width 0.05) on the chain's edges
+    robot, scene = W.chain7_robot(), W.chain7_scene()
+    _, cst, _ = scenes.make_constraint(robot, scene)
+    _, oc, _ = pyoracle.make_constraint(robot, scene)
+    s1, s2 = W.chain7_edges(1024)
+    s1, s2 = np.ascontiguousarray(s1), np.ascontiguousarray(s2)
+    width = np.full(7, 0.05)
+    wptr = C.c_void_p(width.ctypes.data)
+    ok = np.zeros(1, np.uint8)
+    optr = C.c_void_p(ok.ctypes.data)
+    ne = s1.shape[0]
+    got = np.empty(ne, np.uint8)
+    for i in range(20):
+        lib.pmgpu_check_motion(cst._h, C.c_void_p(s1[i].ctypes.data), C.c_void_p(s2[i].ctypes.data), 1, 0, wptr, 0.0, optr, None,
+                               _lib.MEM_HOST, None)
+    p1 = [C.c_void_p(s1[i].ctypes.data) for i in range(ne)]
+    p2 = [C.c_void_p(s2[i].ctypes.data) for i in range(ne)]
+    t0 = time.perf_counter()
+    for i in range(ne):
+        if lib.pmgpu_check_motion(cst._h, p1[i], p2[i], 1, 0, wptr, 0.0, optr, None, _lib.MEM_HOST, None) != 0:
+            raise RuntimeError(lib.pmgpu_last_error().decode())
+        got[i] = ok[0]
+    gpu_us = (time.perf_counter() - t0) / ne * 1e6
+    t0 = time.perf_counter()
+    ref, _ = oc.check_motion(s1, s2, 0, width, threads=1)
+    cpu_us = (time.perf_counter() - t0) / ne * 1e6
+    out["C1"] = {"check_motion_per_call_us": gpu_us, "oracle_single_core_us": cpu_us, "identical": bool(np.array_equal(got, ref)),
+                 "calls": ne}
+    out["what"] = ("per-call latency through the C ABI with host memory (one state / one edge per call, as OMPL's callbacks "
+                   "call), against the oracle's single-core time per state / edge")
+    return out
+
+
+def bench_exact_queries(dev, timed):
+    """The exact FP64 cloud queries outside the fast path: sphere_distances of 4,096 dual-arm
+    configurations (120 spheres each) against the 200k-point cloud, and KDTree.sqdist_batch on 10^5
+    queries near the cloud and 10^5 far from it; beside them the oracle's KD-tree (kdtree.cpp:67-96)
+    on all host cores over the same queries, and whether the squared distances are identical."""
+    import torch
+
+    from oracle import pyoracle
+    from plainmp_gb300 import KDTree, scenes
+
+    W = _workloads()
+    robot, scene = W.dualarm_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0)
+    _, cst, _ = scenes.make_constraint(robot, scene)
+    _, oc, osdf = pyoracle.make_constraint(robot, scene)
+    Q = torch.tensor(W.dualarm_configs(4096, seed=43), device=dev)
+    ms_sd = timed(lambda: cst.sphere_distances(Q), 5)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref_sd = oc.sphere_distances(Q.cpu().numpy(), threads=threads)
+    cpu_sd = time.perf_counter() - t0
+    same_sd = bool(np.array_equal(np.asarray(cst.sphere_distances(Q).cpu()), ref_sd))
+    cloud = scene.cloud.astype(np.float64)
+    rng = np.random.default_rng(44)
+    near = cloud[rng.integers(0, len(cloud), 100000)] + rng.normal(0.0, 0.05, (100000, 3))
+    lo, hi = cloud.min(0), cloud.max(0)
+    far = rng.uniform(lo - 1.5, hi + 1.5, (100000, 3))
+    far = far[np.abs(far - (lo + hi) / 2).max(1) > (hi - lo).max() / 2 + 0.3][:100000]
+    tree = KDTree(cloud)
+    ref_cloud = pyoracle.Sdf.cloud(cloud, 0.0)
+    res = {}
+    for name, pts in (("near", near), ("far", far)):
+        P = torch.tensor(pts, device=dev)
+        ms = timed(lambda: tree.sqdist_batch(P), 5)
+        t0 = time.perf_counter()
+        rsq, _ = ref_cloud.nearest(pts)
+        cpu_s = time.perf_counter() - t0
+        res[name] = {"queries": len(pts), "gpu_ms": ms, "queries_per_s": len(pts) / (ms / 1e3),
+                     "oracle_kdtree_queries_per_s_1_core": len(pts) / cpu_s,
+                     "identical": bool(np.array_equal(np.asarray(tree.sqdist_batch(P).cpu()), rsq))}
+    return {"sphere_distances": {"configs": 4096, "spheres": cst.n_spheres, "gpu_ms": ms_sd,
+                                 "configs_per_s": 4096 / (ms_sd / 1e3), "oracle_configs_per_s": 4096 / cpu_sd,
+                                 "oracle_cores": threads, "identical": same_sd},
+            "kdtree_sqdist_batch": res,
+            "what": "exact FP64 nearest-point queries (cell lists near the cloud, super-blocks elsewhere) vs the oracle KD-tree"}
+
+
 def run_reference(args):
     """The reference arm: the CPU restatement of the reference's is_valid loop (kind "port"; the
     reference itself does not build here) on all host cores, over the whole 65,536-configuration
@@ -798,6 +915,8 @@ def main():
         side = bench_chain7(dev, timed2)
         side["C3"] = bench_ik(dev, timed2, fp32_peak=fma_peaks["fp32_fma_tflops"])
         side["C4"] = bench_traj(dev, timed2)
+        side["exact_queries"] = bench_exact_queries(dev, timed2)
+        side["single_calls"] = bench_single_calls()
 
     if rank != 0:
         return

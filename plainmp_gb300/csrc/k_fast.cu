@@ -301,15 +301,166 @@ constexpr int kOffN = (2 * kOffR + 1) * (2 * kOffR + 1) * (2 * kOffR + 1);
 __device__ char4 c_off[kOffN];     // global memory: lanes read different entries
 __device__ float c_off_lb[kOffN];
 
+// The cell-list search of warp_nearest32 (all 32 lanes, the same query): q's fine cell lists every
+// occupied cell that can hold q's nearest point, nearest first.  32 entries at a time: an entry
+// whose stored lower bound reaches the best so far ends the scan (the list is sorted); the others
+// are tested by their box, and the points of the cells that survive are spread over the lanes (a
+// warp scan of their counts).  best / bidx: the bound and candidate on entry, the result on return.
+// Returns false, touching nothing, where q's cell has no list.  pre: q's list range read ahead
+// (field_corner_record), or x = -2 to read it here.
+__device__ __forceinline__ bool warp_nearest_list32(const PmGridDev& G, float qx, float qy, float qz, float& best, int& bidx,
+                                                    int2 pre = make_int2(-2, -2)) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int2 rng = pre;
+  if (pre.x == -2 && !cell_list_of(G, qx, qy, qz, rng)) return false;
+  if (rng.x < 0) return false;
+  const float unit = G.cell32 * (1.0f / (float)PM_CL_UNITS);
+  for (int base = rng.x; base < rng.y; base += 32) {  // warp-uniform
+    const int k = base + lane;
+    bool beyond = true;  // this entry, and (sorted) every later one, lies beyond the best
+    int2 pr = make_int2(0, 0);
+    if (k < rng.y) {
+      const uint32_t e = __ldg(G.cl_ent + k);
+      const float lbd = (float)(e >> 24) * unit;
+      beyond = lbd * lbd * (1.0f - 1e-5f) >= best;
+      if (!beyond) {
+        const int o = (int)(e & 0xffffffu);
+        const float4 lo = __ldg(G.cell_rec + 2 * o), hi = __ldg(G.cell_rec + 2 * o + 1);
+        const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+        if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < best) pr = make_int2(__float_as_int(lo.w), __float_as_int(hi.w));
+      }
+    }
+    const bool stop = __shfl_sync(FULL, beyond ? 1 : 0, 31) != 0;
+    const int n = pr.y - pr.x;
+    int incl = n;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    for (int t0 = 0; t0 < total; t0 += 32) {  // warp-uniform
+      const int t = t0 + lane;
+      int lo = 0, hi = 31;  // owner: the first lane whose inclusive count exceeds t
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        if (__shfl_sync(FULL, incl, mid) <= t) lo = mid + 1;
+        else hi = mid;
+      }
+      const int own_first = __shfl_sync(FULL, pr.x, lo), own_excl = __shfl_sync(FULL, incl - n, lo);
+      if (t < total) {
+        const int p = own_first + (t - own_excl);
+        const float4 pt = __ldg(G.p32 + p);
+        const float dx = pt.x - qx, dy = pt.y - qy, dz = pt.z - qz;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (d2 < best || (d2 == best && bidx >= 0 && p < bidx)) {
+          best = d2;
+          bidx = p;
+        }
+      }
+    }
+    unsigned long long key = nn_key(best, bidx);
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long k2 = __shfl_xor_sync(FULL, key, o);
+      key = k2 < key ? k2 : key;
+    }
+    best = __uint_as_float((unsigned)(key >> 32));
+    bidx = (int)(unsigned)(key & 0xffffffffu);
+    if (stop) break;
+  }
+  return true;
+}
+
+// warp_nearest_list32 for two queries at once, one per half warp (lanes 0-15 and 16-31), each half
+// scanning its query's list 32 entries at a time (two per lane), so a warp keeps two queries' chains
+// of dependent loads in flight.  Every warp intrinsic runs on all 32 lanes; a half without work (no
+// list, or its scan ended) takes part with empty values.  rng: the half's list range (x < 0: none,
+// the half is left as it is); best / bidx: per half, the bound and candidate on entry (the same on
+// the half's lanes), the result on return.  Same result as warp_nearest_list32.
+__device__ __forceinline__ void halfwarp_list_nearest32(const PmGridDev& G, float qx, float qy, float qz, int2 rng, float& best,
+                                                        int& bidx) {
+  const unsigned FULL = 0xffffffffu;
+  const int hl = threadIdx.x & 15;
+  const float unit = G.cell32 * (1.0f / (float)PM_CL_UNITS);
+  bool live = rng.x >= 0;  // the same on the half's lanes
+  for (int base = 0; __ballot_sync(FULL, live) != 0; base += 32) {  // warp-uniform
+    int2 pr0 = make_int2(0, 0), pr1 = make_int2(0, 0);
+    bool beyond1 = true;  // the lane's second entry; on lane 15 of the half, the chunk's last
+    if (live) {
+      const int k0 = rng.x + base + hl, k1 = k0 + 16;
+      const uint32_t e0 = k0 < rng.y ? __ldg(G.cl_ent + k0) : 0xffffffffu;
+      const uint32_t e1 = k1 < rng.y ? __ldg(G.cl_ent + k1) : 0xffffffffu;
+      const float l0 = (float)(e0 >> 24) * unit, l1 = (float)(e1 >> 24) * unit;
+      const bool beyond0 = k0 >= rng.y || l0 * l0 * (1.0f - 1e-5f) >= best;
+      beyond1 = k1 >= rng.y || l1 * l1 * (1.0f - 1e-5f) >= best;
+      if (!beyond0) {
+        const int o = (int)(e0 & 0xffffffu);
+        const float4 lo = __ldg(G.cell_rec + 2 * o), hi = __ldg(G.cell_rec + 2 * o + 1);
+        const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+        if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < best) pr0 = make_int2(__float_as_int(lo.w), __float_as_int(hi.w));
+      }
+      if (!beyond1) {
+        const int o = (int)(e1 & 0xffffffu);
+        const float4 lo = __ldg(G.cell_rec + 2 * o), hi = __ldg(G.cell_rec + 2 * o + 1);
+        const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+        if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < best) pr1 = make_int2(__float_as_int(lo.w), __float_as_int(hi.w));
+      }
+    }
+    const bool stop = __shfl_sync(FULL, beyond1 ? 1 : 0, 15, 16) != 0;
+    // the points of the surviving cells, spread over the half's lanes
+    const int n0 = pr0.y - pr0.x, n = n0 + (pr1.y - pr1.x);
+    int incl = n;
+    for (int o = 1; o < 16; o <<= 1) {
+      const int t = __shfl_up_sync(FULL, incl, o, 16);
+      if (hl >= o) incl += t;
+    }
+    const int total = __shfl_sync(FULL, incl, 15, 16);
+    const int other = __shfl_xor_sync(FULL, total, 16);
+    const int rounds = total > other ? total : other;  // warp-uniform
+    for (int t0 = 0; t0 < rounds; t0 += 16) {
+      const int t = t0 + hl;
+      int lo = 0, hi = 15;  // owner: the first lane of the half whose inclusive count exceeds t
+      for (int it = 0; it < 4; it++) {
+        const int mid = (lo + hi) >> 1;
+        if (__shfl_sync(FULL, incl, mid, 16) <= t) lo = mid + 1;
+        else hi = mid;
+      }
+      const int own_excl = __shfl_sync(FULL, incl - n, lo, 16);
+      const int own_n0 = __shfl_sync(FULL, n0, lo, 16);
+      const int own_p0 = __shfl_sync(FULL, pr0.x, lo, 16), own_p1 = __shfl_sync(FULL, pr1.x, lo, 16);
+      if (t < total) {
+        const int off = t - own_excl;
+        const int p = off < own_n0 ? own_p0 + off : own_p1 + (off - own_n0);
+        const float4 pt = __ldg(G.p32 + p);
+        const float dx = pt.x - qx, dy = pt.y - qy, dz = pt.z - qz;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (d2 < best || (d2 == best && bidx >= 0 && p < bidx)) {
+          best = d2;
+          bidx = p;
+        }
+      }
+    }
+    unsigned long long key = nn_key(best, bidx);
+    for (int o = 8; o > 0; o >>= 1) {  // within the half
+      const unsigned long long k2 = __shfl_xor_sync(FULL, key, o);
+      key = k2 < key ? k2 : key;
+    }
+    best = __uint_as_float((unsigned)(key >> 32));
+    bidx = (int)(unsigned)(key & 0xffffffffu);
+    live = live && !stop;
+  }
+}
+
 // Warp-cooperative bounded nearest neighbour (FP32): all 32 lanes call it with the same query
 // (and the same optional starting candidate).
-// Blocks are visited nearest-first, 32 offsets at a time, until the next offset's lower bound
+// Where q's fine cell has a cell list, the list answers (warp_nearest_list32).  Elsewhere: the
+// block's candidate list, or the walk below.  Blocks are visited nearest-first, 32 offsets at a time, until the next offset's lower bound
 // clears the current best; every block that may hold a point below the best is handed to all
 // lanes, which split its occupied cells and test their points; the warp minimum is shared after
 // every block.  Result: the exact minimum of the FP32 squared distances below maxd2 (among
 // equal values the smallest sorted index), as grid_nearest32.
 __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2, float init_d2 = INFINITY,
-                                            int init_idx = -1) {
+                                            int init_idx = -1, int2 list_rng = make_int2(-2, -2)) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   NNResult32 r{maxd2, -1};
@@ -318,6 +469,11 @@ __device__ inline NNResult32 warp_nearest32(const PmGridDev& G, float qx, float 
   // walk with a tight bound
   float best = init_d2 < maxd2 ? init_d2 : maxd2;
   int bidx = init_d2 < maxd2 ? init_idx : -1;
+  if (warp_nearest_list32(G, qx, qy, qz, best, bidx, list_rng)) {
+    r.d2 = best;
+    r.idx = bidx;
+    return r;
+  }
   const float reach = sqrtf(maxd2);
   const float blk = G.blk32;
   const float inv = G.inv_blk32;
@@ -609,12 +765,15 @@ __device__ __forceinline__ bool cloud_outside_warp(const PmPrim& P, const PmGrid
   return sqrt(nn.d2) - P.a > r;
 }
 
-// Starting candidate of a warp search, in two steps so that the load can be issued early: the field
+// Starting candidate of a warp search, in two steps so that the loads can be issued early: the field
 // record (nearest point and index) of one of the 8 fine-cell centres around q on lanes 0-7 (index -1
-// elsewhere and outside the grid), then the best of them shared by the warp ((INFINITY, -1) if none).
-__device__ __forceinline__ float4 field_corner_record(const PmGridDev& G, float qx, float qy, float qz) {
-  const int lane = threadIdx.x & 31;
-  float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+// elsewhere and outside the grid), and q's own cell-list range on lane 8 (int bits in x, y; -1 none);
+// then the best of the 8 shared by the warp ((INFINITY, -1) if none) and the list range.
+// sub: the lane's position in its query's group of lanes (the lane itself for a whole warp; 0-15 for
+// a half warp).
+__device__ __forceinline__ float4 field_corner_record(const PmGridDev& G, float qx, float qy, float qz, int sub) {
+  const int lane = sub;
+  float4 rec = make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
   if (lane < 8 && G.n_points > 0) {
     const float inv = G.inv_cell32;
     const float qa[3] = {qx, qy, qz};
@@ -627,14 +786,23 @@ __device__ __forceinline__ float4 field_corner_record(const PmGridDev& G, float 
       cc[a] = ok ? (int)t : 0;
     }
     if (ok) rec = __ldg(G.cell_np + cc[0] + nc[0] * (cc[1] + (int64_t)nc[1] * cc[2]));
+  } else if (lane == 8 && G.n_points > 0) {
+    int2 rng;
+    if (cell_list_of(G, qx, qy, qz, rng)) rec = make_float4(__int_as_float(rng.x), __int_as_float(rng.y), 0.f, __int_as_float(-1));
   }
   return rec;
 }
-__device__ __forceinline__ NNResult32 field_corner_candidate(const float4& rec, float qx, float qy, float qz) {
+struct FieldStart {
+  NNResult32 nn;  // the best of the 8 corner records
+  int2 rng;       // q's cell-list range (-1: none)
+};
+// width: 32 (one query per warp) or 16 (one per half warp; every lane calls it).
+__device__ __forceinline__ FieldStart field_corner_candidate(const float4& rec, float qx, float qy, float qz, int width = 32) {
   const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & (width - 1);
   const int idx = __float_as_int(rec.w);
   unsigned long long key = ~0ull;
-  if (idx >= 0) {  // the FP32 expression of every walk (point_d2_32)
+  if (lane < 8 && idx >= 0) {  // the FP32 expression of every walk (point_d2_32)
     const float dx = rec.x - qx, dy = rec.y - qy, dz = rec.z - qz;
     key = nn_key(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), idx);
   }
@@ -642,13 +810,14 @@ __device__ __forceinline__ NNResult32 field_corner_candidate(const float4& rec, 
     const unsigned long long k2 = __shfl_xor_sync(FULL, key, o);
     key = k2 < key ? k2 : key;
   }
-  key = __shfl_sync(FULL, key, 0);
-  NNResult32 r{INFINITY, -1};
+  key = __shfl_sync(FULL, key, 0, width);
+  const int rx = __shfl_sync(FULL, __float_as_int(rec.x), 8, width), ry = __shfl_sync(FULL, __float_as_int(rec.y), 8, width);
+  FieldStart f{{INFINITY, -1}, make_int2(rx, ry)};
   if (key != ~0ull) {
-    r.d2 = __uint_as_float((unsigned)(key >> 32));
-    r.idx = (int)(unsigned)(key & 0xffffffffu);
+    f.nn.d2 = __uint_as_float((unsigned)(key >> 32));
+    f.nn.idx = (int)(unsigned)(key & 0xffffffffu);
   }
-  return r;
+  return f;
 }
 
 __device__ __forceinline__ int f2o(float f) {
@@ -997,17 +1166,17 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       return xf(P, S.x, S.y, S.z);
     };
     int k = pop();
-    float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    float4 rec = make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
     if (k < nq) {
       const float3 q = centre(k);
-      rec = field_corner_record(v.C[sm.prm[sm.hq[k].y].cloud], q.x, q.y, q.z);
+      rec = field_corner_record(v.C[sm.prm[sm.hq[k].y].cloud], q.x, q.y, q.z, lane);
     }
     while (k < nq) {
       const int kn = pop();
-      float4 rec_n = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+      float4 rec_n = make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
       if (kn < nq) {
         const float3 q = centre(kn);
-        rec_n = field_corner_record(v.C[sm.prm[sm.hq[kn].y].cloud], q.x, q.y, q.z);
+        rec_n = field_corner_record(v.C[sm.prm[sm.hq[kn].y].cloud], q.x, q.y, q.z, lane);
       }
       const int2 e = sm.hq[k];
       const int c = e.x >> 16, si = e.x & 0xffff;
@@ -1024,8 +1193,8 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         const float m = margin32(4.0f + fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z)) + ek;
         const float reach = Pr.a + S.r + (want_dist ? m + cutoff : m);
         const PmGridDev& Gc = v.C[Pr.cloud];
-        const NNResult32 start = field_corner_candidate(rec, sc.x, sc.y, sc.z);
-        const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, start.d2, start.idx);
+        const FieldStart start = field_corner_candidate(rec, sc.x, sc.y, sc.z);
+        const NNResult32 nn = warp_nearest32(Gc, sc.x, sc.y, sc.z, reach * reach, start.nn.d2, start.nn.idx, start.rng);
         if (lane == 0) {
           float g, sd, mag;
           if (nn.idx < 0) {
@@ -1248,45 +1417,72 @@ __device__ __forceinline__ void atomic_min_float(float* a, float v) {
     atomicMax(reinterpret_cast<unsigned int*>(a), __float_as_uint(v));
 }
 
-// The hard cloud queries of a k_fast_valid launch with distances, one warp per query over the whole
-// queue (no per-block barrier), the next query's field records read before the current walk.  Same
-// arithmetic as the in-block answer: the distance goes into dist32 by an exact minimum, a certain
-// collision clears the configuration, an uncertain one goes to the recheck queue.
+// The hard cloud queries of a k_fast_valid launch with distances, two per warp (one per half) over the
+// whole queue (no per-block barrier), the next pair's field records read before the current searches.
+// Same arithmetic as the in-block answer: the distance goes into dist32 by an exact minimum, a certain
+// collision clears the configuration, an uncertain one goes to the recheck queue.  A query whose cell
+// has no list takes the whole warp's search (warp_nearest32) after the pair's list scans.
 template <class Src>
 __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __restrict__ T, const HardQuery* __restrict__ hq,
                                                          float* __restrict__ dist32, Src src, Scratch scr) {
   TView v(T);
-  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
   const int ns = T->n_spheres;
   const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  auto record = [&](int64_t i) {
-    if (i >= n) return make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+  int64_t k = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
+  auto record = [&](int64_t i) {  // the half's query i
+    if (i >= n) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
     const HardQuery h = hq[i];
-    return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z);
+    return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z, hl);
   };
-  float4 rec = record(k);
+  float4 rec = record(k + half);
   while (k < n) {  // warp-uniform
-    const int64_t kn = k + nw;
-    const float4 rec_n = record(kn);
-    const HardQuery h = hq[k];
+    const int64_t kn = k + 2 * nw;
+    const float4 rec_n = record(kn + half);
+    const int64_t i = k + half;
+    const bool have = i < n;  // the same on the half's lanes
+    HardQuery h;
+    h.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    h.b = make_int4(0, 0, 0, 0);
+    if (have) h = hq[i];
     const int cfg = h.b.x, si = h.b.y & 0xffff, prim = (h.b.y >> 16) & 0x7fff;
     const bool check = h.b.y < 0;
     const float ek = __int_as_float(h.b.z);
     const float qx = h.a.x, qy = h.a.y, qz = h.a.z, reach = h.a.w;
     const PmPrim& Pp = v.P[prim];
-    const float pa = (float)Pp.a, sr = (float)v.sr[si];
-    const NNResult32 start = field_corner_candidate(rec, qx, qy, qz);
-    const NNResult32 nn = warp_nearest32(v.C[Pp.cloud], qx, qy, qz, reach * reach, start.d2, start.idx);
-    if (lane == 0) {
+    const int cloud = have ? Pp.cloud : 0;  // a half past the end reads cloud 0's constants only
+    const FieldStart start = field_corner_candidate(rec, qx, qy, qz, 16);
+    const float maxd2 = reach * reach;
+    float best = start.nn.d2 < maxd2 ? start.nn.d2 : maxd2;
+    int bidx = start.nn.d2 < maxd2 ? start.nn.idx : -1;
+    const bool nonfinite = !isfinite(qx) || !isfinite(qy) || !isfinite(qz);
+    const int2 rng = have && !nonfinite ? start.rng : make_int2(-1, -1);
+    halfwarp_list_nearest32(v.C[cloud], qx, qy, qz, rng, best, bidx);
+    // a query without a list: the whole warp's search, one half at a time
+    const bool need = have && rng.x < 0;
+    for (int hh = 0; hh < 2; hh++) {
+      if (__shfl_sync(FULL, need ? 1 : 0, 16 * hh) != 0) {  // warp-uniform
+        const float bx = __shfl_sync(FULL, qx, 16 * hh), by = __shfl_sync(FULL, qy, 16 * hh), bz = __shfl_sync(FULL, qz, 16 * hh);
+        const float bm = __shfl_sync(FULL, maxd2, 16 * hh), bd = __shfl_sync(FULL, start.nn.d2, 16 * hh);
+        const int bi = __shfl_sync(FULL, start.nn.idx, 16 * hh), bc = __shfl_sync(FULL, cloud, 16 * hh);
+        const NNResult32 r = warp_nearest32(v.C[bc], bx, by, bz, bm, bd, bi, make_int2(-1, -1));
+        if (half == hh) {
+          best = r.d2;
+          bidx = r.idx;
+        }
+      }
+    }
+    if (have && hl == 0) {
+      const float pa = (float)Pp.a, sr = (float)v.sr[si];
       float g, sd, mag;
-      if (nn.idx < 0) {
+      if (bidx < 0) {
         g = reach - pa - sr;
         sd = 3.0e38f;
         mag = fabsf(qx) + fabsf(qy) + fabsf(qz);
       } else {
-        const float d = sqrtf(nn.d2);
+        const float d = sqrtf(best);
         g = d - pa - sr;
         sd = g;
         mag = fabsf(qx) + fabsf(qy) + fabsf(qz) + d;
@@ -1297,7 +1493,7 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
         if (g < -mm) {
           src.fail(cfg);
         } else if (g <= mm) {
-          push_item(scr, src, cfg, prim << 1, si, nn.idx);
+          push_item(scr, src, cfg, prim << 1, si, bidx);
         }
       }
     }

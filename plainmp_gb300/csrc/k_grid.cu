@@ -349,6 +349,169 @@ __global__ void k_blk_ranges(const float* __restrict__ R, const int32_t* __restr
   out[b] = R[b] < 0.f ? make_int2(-1, -1) : make_int2(start[b], start[b] + cnt[b]);
 }
 
+// Per-fine-cell lists of occupied cells, built per grid block (one CTA of kClThreads, 64 fine
+// cells).  A query q in cell c (up to the FP32 rounding of its cell, covered by 1e-5 m of slack on
+// the cell's box) has a point within
+//   ub(c) = |q - p(c)| <= half cell diagonal + |c - p(c)|
+// (p(c): the nearest point of the cell centre, from the field), so only the occupied cells whose
+// box lies within ub(c) of c's box can hold its nearest point.  The CTA stages in shared memory
+// the occupied cells within U = max ub(c) of the block's box, found on the block's candidate list
+// (which covers blk_reach >= U); each warp then takes fine cells of the block and filters the
+// staged cells by their distance from the cell's box.  Cells without a field point, with ub(c)
+// above list_reach or beyond their block's reach, and the cells of a block whose candidates do
+// not fit kClStage get no list (the queries there take the block walk).
+// pass 0: count per cell (0: no list) and the 64-bit total; pass 1: the entries, unsorted into
+// tmp, then ranked by (distance, record) into out.
+constexpr int kClThreads = 256;
+constexpr int kClStage = 3072;  // staged candidate cells per block (28 B each)
+constexpr size_t kClSmem = (size_t)kClStage * 28;
+__global__ void __launch_bounds__(kClThreads) k_cell_lists(PmGridDev G, int pass, float list_reach, int32_t* __restrict__ cnt,
+                                                           const int32_t* __restrict__ start, uint2* __restrict__ tmp,
+                                                           uint32_t* __restrict__ out, unsigned long long* __restrict__ total) {
+  extern __shared__ __align__(16) float cl_smem[];  // kClSmem bytes: the staged boxes, then their records
+  float* s_box = cl_smem;
+  int* s_id = reinterpret_cast<int*>(cl_smem + kClStage * 6);
+  __shared__ float s_ub[PM_GRID_CELLS_PER_BLOCK];
+  __shared__ int s_n, s_umax, s_over;
+  const unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t b = blockIdx.x;
+  const int bx = (int)(b % G.nbx), by = (int)((b / G.nbx) % G.nby), bz = (int)(b / ((int64_t)G.nbx * G.nby));
+  const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
+  const float cell = G.cell32;
+  const int2 rng = G.blk_list[b];
+  const float rb = G.blk_reach[b];
+  if (tid == 0) {
+    s_n = 0;
+    s_umax = 0;
+    s_over = 0;
+  }
+  __syncthreads();
+  // 1. ub per fine cell of the block (local index x fastest), -1: no list
+  auto cell_index = [&](int l, int& cx, int& cy, int& cz) {
+    cx = bx * PM_GRID_B + l % PM_GRID_B;
+    cy = by * PM_GRID_B + (l / PM_GRID_B) % PM_GRID_B;
+    cz = bz * PM_GRID_B + l / (PM_GRID_B * PM_GRID_B);
+    return cx + (int64_t)nc[0] * (cy + (int64_t)nc[1] * cz);
+  };
+  if (tid < PM_GRID_CELLS_PER_BLOCK) {
+    int cx, cy, cz;
+    const int64_t i = cell_index(tid, cx, cy, cz);
+    const int2 nn = G.cell_nn[i];
+    float ub = -1.f;
+    if (nn.y >= 0 && rng.x >= 0) {
+      const float4 p = G.p32[nn.y];
+      const float dx = p.x - field_centre(G.o32[0], cx, cell), dy = p.y - field_centre(G.o32[1], cy, cell),
+                  dz = p.z - field_centre(G.o32[2], cz, cell);
+      ub = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * 1.00001f + 0.8660254f * cell * 1.00001f + 3e-5f;
+      if (!(ub <= list_reach) || !(ub <= rb)) ub = -1.f;
+    }
+    s_ub[tid] = ub;
+    if (ub >= 0.f) atomicMax(&s_umax, __float_as_int(ub));  // non-negative floats order as their bits
+  }
+  __syncthreads();
+  const float U = __int_as_float(s_umax);
+  if (U <= 0.f) {  // block-uniform: no cell of the block gets a list
+    if (pass == 0 && tid < PM_GRID_CELLS_PER_BLOCK) {
+      int cx, cy, cz;
+      cnt[cell_index(tid, cx, cy, cz)] = 0;
+    }
+    return;
+  }
+  // 2. stage the occupied cells within U of the block's box (entries sorted by block distance)
+  const float slack = 1e-5f, blk = G.blk32;
+  const float blo[3] = {G.o32[0] + (float)bx * blk - slack, G.o32[1] + (float)by * blk - slack, G.o32[2] + (float)bz * blk - slack};
+  const float bhi[3] = {blo[0] + blk + 2.f * slack, blo[1] + blk + 2.f * slack, blo[2] + blk + 2.f * slack};
+  for (int k = rng.x + warp; k < rng.y; k += kClThreads / 32) {  // warp per entry
+    const int4 e = G.cand4[k];
+    if (__int_as_float(e.w) > U * 1.0001f + 1e-6f) break;  // warp-uniform; later entries are farther
+    for (int base = e.x; base < e.y; base += 32) {
+      const int o = base + lane;
+      if (o < e.y) {
+        const float* cb = G.cell_box + 6 * (int64_t)o;
+        if (box_box_d(blo, bhi, cb) * (1.0f - 1e-6f) <= U) {
+          const int slot = atomicAdd(&s_n, 1);
+          if (slot < kClStage) {
+            s_id[slot] = o;
+            for (int a = 0; a < 6; a++) s_box[6 * slot + a] = cb[a];
+          } else {
+            s_over = 1;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const int n_stage = min(s_n, kClStage);
+  const bool over = s_over != 0;
+  const float to_units = (float)PM_CL_UNITS / cell;
+  // 3. per fine cell (warp-strided): filter the staged cells by the distance from the cell's box
+  for (int l = warp; l < PM_GRID_CELLS_PER_BLOCK; l += kClThreads / 32) {
+    int cx, cy, cz;
+    const int64_t i = cell_index(l, cx, cy, cz);
+    const float ub = over ? -1.f : s_ub[l];
+    if (ub < 0.f) {  // warp-uniform
+      if (pass == 0 && lane == 0) cnt[i] = 0;
+      continue;
+    }
+    const int room = pass == 1 ? cnt[i] : 0;  // pass 1 fills the room pass 0 counted
+    if (pass == 1 && room <= 0) continue;
+    const float lo[3] = {G.o32[0] + (float)cx * cell - slack, G.o32[1] + (float)cy * cell - slack, G.o32[2] + (float)cz * cell - slack};
+    const float hi[3] = {lo[0] + cell + 2.f * slack, lo[1] + cell + 2.f * slack, lo[2] + cell + 2.f * slack};
+    const int64_t s0 = pass == 1 ? start[i] : 0;
+    int n = 0;
+    for (int base = 0; base < n_stage; base += 32) {
+      const int j = base + lane;
+      float d = 0.f;
+      bool in = false;
+      if (j < n_stage) {
+        d = box_box_d(lo, hi, s_box + 6 * j) * (1.0f - 1e-6f);
+        in = d <= ub;
+      }
+      const unsigned bal = __ballot_sync(FULL, in);
+      if (pass == 1 && in) {
+        const int pos = n + __popc(bal & ((1u << lane) - 1u));
+        if (pos < room) tmp[s0 + pos] = make_uint2((unsigned)s_id[j], __float_as_uint(d));
+      }
+      n += __popc(bal);
+    }
+    if (pass == 0) {
+      if (n > 1024) n = 0;  // a list this long is not worth its scan (or its build-time sort): the cell takes the block walk
+      if (lane == 0) {
+        cnt[i] = n;
+        atomicAdd(total, (unsigned long long)n);  // 64-bit: the int32 scan is used only below 2^30
+      }
+      continue;
+    }
+    __syncwarp();
+    n = min(n, room);  // equal: both passes stage and filter the same cells
+    // rank of each entry by (distance, record): every order has a unique place
+    for (int j = lane; j < n; j += 32) {
+      const uint2 ej = tmp[s0 + j];
+      const float dj = __uint_as_float(ej.y);
+      int r = 0;
+      for (int k = 0; k < n; k++) {
+        const uint2 ek = tmp[s0 + k];
+        const float dk = __uint_as_float(ek.y);
+        r += (dk < dj || (dk == dj && ek.x < ej.x)) ? 1 : 0;
+      }
+      const float u = floorf(dj * to_units * (1.0f - 1e-6f));
+      const unsigned q = u >= 255.f ? 255u : (u > 0.f ? (unsigned)u : 0u);
+      out[s0 + r] = ej.x | (q << 24);
+    }
+    // should the passes ever differ, the rest of the room still holds valid records (record 0 at the
+    // largest bound)
+    for (int j = n + lane; j < room; j += 32) out[s0 + j] = 0u | (255u << 24);
+    __syncwarp();
+  }
+}
+
+__global__ void k_cl_ranges(const int32_t* __restrict__ cnt, const int32_t* __restrict__ start, int64_t n, int2* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = cnt[i] > 0 ? make_int2(start[i], start[i] + cnt[i]) : make_int2(-1, -1);
+}
+
 inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 // FP32 roundings of a double toward -inf / +inf (host)
 inline float round_down_f(double v) {
@@ -423,6 +586,13 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   float4* cand_box = nullptr;
   int2* blk_list = nullptr;
   int2* blk_cand = nullptr;
+  int2* cl_rng = nullptr;
+  uint32_t* cl_ent = nullptr;
+  int64_t n_cl = 0;
+  int2* sb_rng = nullptr;
+  int32_t* sb_blk = nullptr;
+  float* sb_box = nullptr;
+  int32_t n_sb = 0;
   float* blk_reach = nullptr;
   int32_t n_cand = 0;
   float *blk_box = nullptr, *cell_box = nullptr;
@@ -466,6 +636,47 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     k_block_records<<<nblk(nblocks, 128), 128, 0, s>>>(recidx, nblocks, n_rec, cell_box, blk_occ, blk_box);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
+    {  // super-blocks of PM_GRID_SB^3 blocks (host: a few thousand at most): the non-empty ones, each
+       // with its occupied blocks and the box of its points
+      std::vector<int32_t> h_occ((size_t)nblocks * 2);
+      std::vector<float> h_box((size_t)nblocks * 6);
+      if ((e = cudaMemcpyAsync(h_occ.data(), blk_occ, h_occ.size() * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+      if ((e = cudaMemcpyAsync(h_box.data(), blk_box, h_box.size() * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+      const int ns[3] = {(nb[0] + PM_GRID_SB - 1) / PM_GRID_SB, (nb[1] + PM_GRID_SB - 1) / PM_GRID_SB, (nb[2] + PM_GRID_SB - 1) / PM_GRID_SB};
+      std::vector<std::vector<int32_t>> members((size_t)ns[0] * ns[1] * ns[2]);
+      for (int64_t b = 0; b < nblocks; b++) {
+        if (h_occ[2 * b] >= h_occ[2 * b + 1]) continue;
+        const int bx = (int)(b % nb[0]), by = (int)((b / nb[0]) % nb[1]), bz = (int)(b / ((int64_t)nb[0] * nb[1]));
+        members[(bx / PM_GRID_SB) + (size_t)ns[0] * ((by / PM_GRID_SB) + (size_t)ns[1] * (bz / PM_GRID_SB))].push_back((int32_t)b);
+      }
+      std::vector<int2> h_rng;
+      std::vector<int32_t> h_blk;
+      std::vector<float> h_sbox;
+      for (auto& m : members) {
+        if (m.empty()) continue;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int32_t b : m)
+          for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], h_box[6 * (size_t)b + a]);
+            hi[a] = std::max(hi[a], h_box[6 * (size_t)b + 3 + a]);
+          }
+        h_rng.push_back(make_int2((int)h_blk.size(), (int)(h_blk.size() + m.size())));
+        h_blk.insert(h_blk.end(), m.begin(), m.end());
+        for (int a = 0; a < 3; a++) h_sbox.push_back(lo[a]);
+        for (int a = 0; a < 3; a++) h_sbox.push_back(hi[a]);
+      }
+      n_sb = (int32_t)h_rng.size();
+      if ((e = keep(std::max<size_t>(h_rng.size(), 1) * 8, (void**)&sb_rng)) != cudaSuccess) break;
+      if ((e = keep(std::max<size_t>(h_blk.size(), 1) * 4, (void**)&sb_blk)) != cudaSuccess) break;
+      if ((e = keep(std::max<size_t>(h_sbox.size(), 1) * 4, (void**)&sb_box)) != cudaSuccess) break;
+      if (n_sb > 0) {
+        if ((e = cudaMemcpyAsync(sb_rng, h_rng.data(), h_rng.size() * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(sb_blk, h_blk.data(), h_blk.size() * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(sb_box, h_sbox.data(), h_sbox.size() * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;  // the host vectors go out of scope
+      }
+    }
     {
       int16_t *t0 = nullptr, *t1 = nullptr;
       if ((e = scratch(nblocks * 2, (void**)&t0)) != cudaSuccess) break;
@@ -500,6 +711,14 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       v.blk_list = nullptr;  // the walks below run without candidate lists
       v.blk_cand = nullptr;
       v.blk_reach = nullptr;
+      v.cand4 = nullptr;
+      v.cand_box = nullptr;
+      v.cl_rng = nullptr;
+      v.cl_ent = nullptr;
+      v.sb_rng = sb_rng;
+      v.sb_blk = sb_blk;
+      v.sb_box = sb_box;
+      v.n_sb = n_sb;
       v.px = px;
       v.py = py;
       v.pz = pz;
@@ -537,6 +756,43 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       if ((e = keep((size_t)std::max<int32_t>(n_cand, 1) * 32, (void**)&cand_box)) != cudaSuccess) break;
       if (n_cand > 0) k_cand_expand<<<nblk(n_cand, 256), 256, 0, s>>>(blk_cand, n_cand, blk_occ, blk_box, cand4, cand_box);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
+      // per-fine-cell lists (record indices must fit their 24 bits); ncl: the fine cells, as above
+      if ((e = keep((size_t)ncl * 8, (void**)&cl_rng)) != cudaSuccess) break;
+      if (g.list_reach > 0.0 && n_rec < (1 << 24) && n_cand > 0) {
+        v.blk_list = blk_list;
+        v.blk_cand = blk_cand;
+        v.blk_reach = blk_reach;
+        v.cand4 = cand4;
+        v.cand_box = cand_box;
+        int32_t *ccnt = nullptr, *cstart = nullptr;
+        unsigned long long* ctot = nullptr;
+        if ((e = scratch((size_t)ncl * 4, (void**)&ccnt)) != cudaSuccess) break;
+        if ((e = scratch((size_t)ncl * 4, (void**)&cstart)) != cudaSuccess) break;
+        if ((e = scratch(8, (void**)&ctot)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(ctot, 0, 8, s)) != cudaSuccess) break;
+        if ((e = cudaFuncSetAttribute(k_cell_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClSmem)) != cudaSuccess) break;
+        k_cell_lists<<<(unsigned)nblocks, kClThreads, kClSmem, s>>>(v, 0, (float)g.list_reach, ccnt, nullptr, nullptr, nullptr, ctot);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        unsigned long long total = 0;
+        if ((e = cudaMemcpyAsync(&total, ctot, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+        n_cl = (int64_t)total;
+        uint2* cl_tmp = nullptr;
+        if (n_cl > 0 && n_cl < ((int64_t)1 << 30)) {  // the int32 scan below holds it
+          if ((e = exclusive_scan(ccnt, ncl, cstart, s, tmp)) != cudaSuccess) break;
+          if ((e = keep((size_t)n_cl * 4, (void**)&cl_ent)) != cudaSuccess) break;
+          if ((e = scratch((size_t)n_cl * 8, (void**)&cl_tmp)) != cudaSuccess) break;
+          k_cell_lists<<<(unsigned)nblocks, kClThreads, kClSmem, s>>>(v, 1, (float)g.list_reach, ccnt, cstart, cl_tmp, cl_ent, nullptr);
+          if ((e = cudaGetLastError()) != cudaSuccess) break;
+          k_cl_ranges<<<nblk(ncl, 256), 256, 0, s>>>(ccnt, cstart, ncl, cl_rng);
+        } else {
+          n_cl = 0;
+          if ((e = cudaMemsetAsync(cl_rng, 0xff, (size_t)ncl * 8, s)) != cudaSuccess) break;
+        }
+      } else {
+        if ((e = cudaMemsetAsync(cl_rng, 0xff, (size_t)ncl * 8, s)) != cudaSuccess) break;
+      }
+      if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
     e = cudaStreamSynchronize(s);
   } while (false);
@@ -563,6 +819,13 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.blk_reach = blk_reach;
   d.cand4 = cand4;
   d.cand_box = cand_box;
+  d.cl_rng = cl_rng;
+  d.cl_ent = cl_ent;
+  d.sb_rng = sb_rng;
+  d.sb_blk = sb_blk;
+  d.sb_box = sb_box;
+  d.n_sb = n_sb;
+  g.n_cell_list = n_cl;
   g.n_occupied = n_rec;
   g.n_cand = n_cand;
   d.field_reach = (float)g.field_reach;

@@ -15,6 +15,8 @@
 #define PM_MAX_CLOUDS 8
 #define PM_GRID_B 4  // fine cells per block edge of the point-cloud grid
 #define PM_GRID_CELLS_PER_BLOCK (PM_GRID_B * PM_GRID_B * PM_GRID_B)
+#define PM_CL_UNITS 16  // distance quantum of the cell lists: the fine cell edge / 16
+#define PM_GRID_SB 4    // blocks per super-block edge (the coarse level of the unbounded searches)
 
 enum { PM_FK_STATE = 0, PM_FK_REV = 1, PM_FK_PRIS = 2 };
 enum { PM_BASE_FIXED = 0, PM_BASE_FLOATING = 1, PM_BASE_PLANAR = 2 };
@@ -96,6 +98,16 @@ struct PmGridDev {
   const int4* cand4;       // blk_cand widened for the warp searches: (first occupied-cell record, end, block,
                            // float bits of the distance), so one load gives the cell range
   const float4* cand_box;  // per list entry, its block's box: (lo xyz, 0), (hi xyz, 0)
+  const int2* cl_rng;      // per fine cell (x fastest): [first, end) of its cell list in cl_ent (first = -1: none)
+  const uint32_t* cl_ent;  // cell lists, nearest first: occupied-cell record (low 24 bits) | a lower bound on the
+                           // distance between that record's box and the listing cell's box, in units of
+                           // cell / PM_CL_UNITS, rounded down and capped at 255 (high 8 bits); a cell's list holds
+                           // every occupied cell that can contain the nearest point of a query inside it
+  const int2* sb_rng;      // per non-empty super-block (PM_GRID_SB^3 blocks): [first, end) of its occupied blocks in sb_blk
+  const int32_t* sb_blk;   // occupied blocks, grouped by super-block
+  const float* sb_box;     // per non-empty super-block: box of its points (lo xyz, hi xyz)
+  int32_t n_sb;            // non-empty super-blocks
+  int32_t pad_sb;
   // FP32 copies for the FP32 queries (no FP64 arithmetic on their path): origin, block edge and
   // its reciprocal, fine cell edge and its reciprocal, and the points' box (rounded outwards)
   float o32[3], blk32, inv_blk32, cell32, inv_cell32;

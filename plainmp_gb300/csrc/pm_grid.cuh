@@ -4,9 +4,12 @@
 // Layout (built by k_grid.cu): blocks of PM_GRID_B^3 fine cells; each occupied fine cell has
 // a conservative FP32 bounding box of its points (lo rounded down, hi rounded up) and a
 // contiguous point range; each block has the union box and its range of occupied-cell
-// records.  A query walks Chebyshev rings of blocks around the query's (clamped) block,
-// skips blocks and cells whose box is at least as far as the best distance so far, and
-// stops once every unvisited block lies beyond the best distance.
+// records; super-blocks of PM_GRID_SB^3 blocks list their occupied blocks.  Near the cloud,
+// a fine cell's list names every occupied cell that can hold the nearest point of a query
+// inside it, nearest first, and a query scans it until the stored lower bound reaches the best
+// distance.  Elsewhere the FP64 query visits the super-blocks by box distance, and the bounded
+// FP32 query walks Chebyshev rings of blocks around the query's (clamped) block; both skip
+// boxes at least as far as the best distance so far.
 //
 // Exactness: the squared distance of a point is fl(dx*dx + (dy*dy + dz*dz)) with d = p - q,
 // as the KD-tree computes it (kdtree.cpp:125).  The box distance uses the same formula on
@@ -38,80 +41,98 @@ struct NNResult64 {
   int32_t idx;  // sorted point index, -1 if the cloud is empty
 };
 
-// Exact FP64 nearest squared distance among the points with squared distance below maxd2
-// (idx = -1 when there is none).  The walk starts at the ring of the nearest occupied block
-// (rings inside it hold no point) and is bounded by the grid size.
-__device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q, double maxd2 = INFINITY) {
-  NNResult64 r{maxd2, -1};
-  // a NaN or infinite query is farther than every bound from every point (the KD-tree's
-  // comparisons all fail the same way); it must not reach the block arithmetic below
-  if (G.n_points <= 0 || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z)) return r;
-  const double inv = 1.0 / G.block;
-  int cb[3];
-  const double qa[3] = {q.x, q.y, q.z};
-  const int nb[3] = {G.nbx, G.nby, G.nbz};
-  bool inside = true;
+// The fine cell of q (FP32 arithmetic, the expression the cell lists were built against) and its
+// cell list range; false where q lies outside the grid or its cell has no list.
+__device__ __forceinline__ bool cell_list_of(const PmGridDev& G, float qx, float qy, float qz, int2& rng) {
+  if (G.cl_rng == nullptr) return false;
+  const float qa[3] = {qx, qy, qz};
+  const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
+  int cc[3];
   for (int a = 0; a < 3; a++) {
-    double f = floor((qa[a] - G.origin[a]) * inv);
-    if (!(f >= 0 && f <= nb[a] - 1)) inside = false;
-    int c = !(f >= 0) ? 0 : (f > nb[a] - 1 ? nb[a] - 1 : (int)f);
-    cb[a] = c;
+    const float t = floorf((qa[a] - G.o32[a]) * G.inv_cell32);
+    if (!(t >= 0.f && t <= (float)(nc[a] - 1))) return false;
+    cc[a] = (int)t;
   }
-  const int k0 = G.edf[cb[0] + nb[0] * (cb[1] + nb[1] * cb[2])];
-  if (inside && k0 >= 2) {  // every point lies at least (k0 - 1) blocks away from q's block
-    const double lb0 = (double)(k0 - 1) * G.block - 1e-9;
-    if (lb0 > 0 && lb0 * lb0 >= r.d2) return r;
+  rng = __ldg(G.cl_rng + (cc[0] + nc[0] * (cc[1] + (int64_t)nc[1] * cc[2])));
+  return rng.x >= 0;
+}
+
+// FP64 scan of q's cell list (nearest first; the scan ends at the first entry whose stored lower
+// bound reaches the best).  The list holds every occupied cell that can contain q's nearest point
+// (built with 3e-5 m of slack, far above the FP32 / FP64 difference of q's cell assignment), so
+// the result is the global exact minimum.
+__device__ inline bool list_nearest64(const PmGridDev& G, const D3& q, NNResult64& r) {
+  int2 rng;
+  if (!cell_list_of(G, (float)q.x, (float)q.y, (float)q.z, rng)) return false;
+  const double unit = (double)G.cell32 * (1.0 / PM_CL_UNITS);
+  for (int k = rng.x; k < rng.y; k++) {
+    const uint32_t e = __ldg(G.cl_ent + k);
+    const double lbd = (double)(e >> 24) * unit;
+    if (lbd * lbd * (1.0 - 1e-9) >= r.d2) break;  // sorted: no later entry comes closer
+    const int c = (int)(e & 0xffffffu);
+    if (box_d2_64(G.cell_box + 6 * (int64_t)c, q) >= r.d2) continue;
+    const int p0 = G.cell_pts[2 * c], p1 = G.cell_pts[2 * c + 1];
+    for (int i = p0; i < p1; i++) {
+      D3 d{G.px[i] - q.x, G.py[i] - q.y, G.pz[i] - q.z};
+      double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
+      if (d2 < r.d2) {
+        r.d2 = d2;
+        r.idx = i;
+      }
+    }
   }
-  const int kmax = max(nb[0], max(nb[1], nb[2]));
-  for (int K = min(k0, kmax); K <= kmax; K++) {
-    const int z0 = max(cb[2] - K, 0), z1 = min(cb[2] + K, nb[2] - 1);
-    const int y0 = max(cb[1] - K, 0), y1 = min(cb[1] + K, nb[1] - 1);
-    const int x0 = max(cb[0] - K, 0), x1 = min(cb[0] + K, nb[0] - 1);
-    for (int bz = z0; bz <= z1; bz++) {
-      const bool zf = (bz == cb[2] - K) || (bz == cb[2] + K);
-      for (int by = y0; by <= y1; by++) {
-        const bool yf = zf || (by == cb[1] - K) || (by == cb[1] + K);
-        const int step = yf ? 1 : 2 * K;
-        for (int bx = (yf ? x0 : cb[0] - K); bx <= x1; bx += (step > 0 ? step : 1)) {
-          if (bx < x0) continue;
-          const int b = bx + nb[0] * (by + nb[1] * bz);
-          const int c0 = G.blk_occ[2 * b], c1 = G.blk_occ[2 * b + 1];
-          if (c0 >= c1) continue;
-          if (box_d2_64(G.blk_box + 6 * b, q) >= r.d2) continue;
-          for (int c = c0; c < c1; c++) {
-            if (box_d2_64(G.cell_box + 6 * c, q) >= r.d2) continue;
-            const int p0 = G.cell_pts[2 * c], p1 = G.cell_pts[2 * c + 1];
-            for (int i = p0; i < p1; i++) {
-              D3 d{G.px[i] - q.x, G.py[i] - q.y, G.pz[i] - q.z};
-              double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
-              if (d2 < r.d2) {
-                r.d2 = d2;
-                r.idx = i;
-              }
-            }
+  return true;
+}
+
+// FP64 search over the super-blocks, for queries without a cell list (far from the cloud or
+// outside the grid): the super-block with the smallest box distance first, then every other
+// super-block whose box is closer than the best; inside one, its occupied blocks, their cells and
+// points, each skipped when its box is not closer than the best.
+__device__ inline void sb_nearest64(const PmGridDev& G, const D3& q, NNResult64& r) {
+  auto visit = [&](int j) {
+    const int2 br = __ldg(G.sb_rng + j);
+    for (int k = br.x; k < br.y; k++) {
+      const int b = __ldg(G.sb_blk + k);
+      if (box_d2_64(G.blk_box + 6 * (int64_t)b, q) >= r.d2) continue;
+      const int c0 = G.blk_occ[2 * b], c1 = G.blk_occ[2 * b + 1];
+      for (int c = c0; c < c1; c++) {
+        if (box_d2_64(G.cell_box + 6 * (int64_t)c, q) >= r.d2) continue;
+        const int p0 = G.cell_pts[2 * c], p1 = G.cell_pts[2 * c + 1];
+        for (int i = p0; i < p1; i++) {
+          D3 d{G.px[i] - q.x, G.py[i] - q.y, G.pz[i] - q.z};
+          double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
+          if (d2 < r.d2) {
+            r.d2 = d2;
+            r.idx = i;
           }
-          if (K == 0) break;
         }
       }
     }
-    // lower bound for blocks outside the visited cube
-    double lb = INFINITY;
-    for (int a = 0; a < 3; a++) {
-      if (cb[a] - K - 1 >= 0) {
-        double face = G.origin[a] + (double)(cb[a] - K) * G.block;
-        lb = fmin(lb, qa[a] - face);
-      }
-      if (cb[a] + K + 1 <= nb[a] - 1) {
-        double face = G.origin[a] + (double)(cb[a] + K + 1) * G.block;
-        lb = fmin(lb, face - qa[a]);
-      }
+  };
+  double lb_min = INFINITY;
+  int j_min = -1;
+  for (int j = 0; j < G.n_sb; j++) {
+    const double lb = box_d2_64(G.sb_box + 6 * (int64_t)j, q);
+    if (lb < lb_min) {
+      lb_min = lb;
+      j_min = j;
     }
-    if (lb == INFINITY) break;  // the cube covers the grid
-    // nominal block faces carry the rounding of the build-time block assignment (~1e-16 m):
-    // stop only when the bound minus 1 nm still clears the best distance
-    const double lbm = lb - 1e-9;
-    if (lbm > 0 && lbm * lbm >= r.d2) break;
   }
+  if (j_min < 0 || !(lb_min < r.d2)) return;
+  visit(j_min);
+  for (int j = 0; j < G.n_sb; j++)
+    if (j != j_min && box_d2_64(G.sb_box + 6 * (int64_t)j, q) < r.d2) visit(j);
+}
+
+// Exact FP64 nearest squared distance among the points with squared distance below maxd2
+// (idx = -1 when there is none): q's cell list where it has one, else the super-blocks.
+__device__ inline NNResult64 grid_nearest64(const PmGridDev& G, const D3& q, double maxd2 = INFINITY) {
+  NNResult64 r{maxd2, -1};
+  // a NaN or infinite query is farther than every bound from every point (the KD-tree's
+  // comparisons all fail the same way); it must not reach the index arithmetic below
+  if (G.n_points <= 0 || !isfinite(q.x) || !isfinite(q.y) || !isfinite(q.z)) return r;
+  if (list_nearest64(G, q, r)) return r;
+  sb_nearest64(G, q, r);
   return r;
 }
 
@@ -131,6 +152,29 @@ __device__ __forceinline__ float box_d2_32(const float* b, float qx, float qy, f
 __device__ inline NNResult32 grid_nearest32(const PmGridDev& G, float qx, float qy, float qz, float maxd2 = INFINITY) {
   NNResult32 r{maxd2, -1};
   if (G.n_points <= 0 || !isfinite(qx) || !isfinite(qy) || !isfinite(qz)) return r;  // as grid_nearest64
+  int2 crng;
+  if (cell_list_of(G, qx, qy, qz, crng)) {  // q's cell list: every cell that can hold its nearest point
+    const float unit = G.cell32 * (1.0f / (float)PM_CL_UNITS);
+    for (int k = crng.x; k < crng.y; k++) {
+      const uint32_t e = __ldg(G.cl_ent + k);
+      const float lbd = (float)(e >> 24) * unit;
+      if (lbd * lbd * (1.0f - 1e-5f) >= r.d2) break;
+      const int c = (int)(e & 0xffffffu);
+      const float4 lo = __ldg(G.cell_rec + 2 * c), hi = __ldg(G.cell_rec + 2 * c + 1);
+      const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+      if (fmaf(gx, gx, fmaf(gy, gy, gz * gz)) >= r.d2) continue;
+      for (int i = __float_as_int(lo.w); i < __float_as_int(hi.w); i++) {
+        const float4 p = __ldg(G.p32 + i);
+        const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (d2 < r.d2 || (d2 == r.d2 && r.idx >= 0 && i < r.idx)) {
+          r.d2 = d2;
+          r.idx = i;
+        }
+      }
+    }
+    return r;
+  }
   const float inv = G.inv_blk32;
   const float ox = G.o32[0], oy = G.o32[1], oz = G.o32[2];
   const float blk = G.blk32;

@@ -104,12 +104,13 @@ struct GridBuild {
   double radius;
   double cell;  // fine cell edge
   double field_reach = 0.3;  // nearest-point field: search radius around each cell centre
+  double list_reach = 0.25;  // per-cell lists for the cells whose nearest-point bound is below this
   // outputs (owned by the caller after the call; freed with grid_free)
   PmGridDev dev;
-  void* allocs[24];
+  void* allocs[28];
   int n_allocs;
   // sizes of what was built: occupied fine cells, candidate-list entries, device bytes kept
-  int64_t n_occupied = 0, n_cand = 0, bytes = 0;
+  int64_t n_occupied = 0, n_cand = 0, bytes = 0, n_cell_list = 0;
 };
 // Builds the grid synchronously on `s` (allocates device memory); returns cudaSuccess or the
 // first CUDA error.  host_lb/host_ub receive the CloudSDF AABB.

@@ -370,3 +370,26 @@ def test_fast_degenerate_clouds(oracle):
         assert np.array_equal(ok, ref), len(pts)
         d_ref = np.minimum(cst.sphere_distances(Q), CUTOFF)
         assert np.abs(d.astype(np.float64) - d_ref).max() < DIST_TOL, len(pts)
+
+
+def test_fast_queries_beyond_the_cell_lists(oracle):
+    """Spheres twice as large (up to 0.16 m) and a 0.05 m cloud radius, no self pairs: hard cloud
+    queries reach 0.31 m, so they come from cells both within and beyond the cell lists' 0.25 m,
+    and the lists and the whole-warp search both answer.  Validity equals the oracle and the plain
+    method in both modes; distances are within the bound of the plain FP64 distances."""
+    base = W.dualarm_robot()
+    big = [W.SphereSpec(s.parent_link_name, s.relative_positions, s.radii * 2.0, s.only_self_collision) for s in base.spheres]
+    robot = W.Robot(base.urdf, base.control_joints, base.end_link, big, base.self_pairs)
+    scene = W.Scene(cloud=W.box_surface_cloud(n_points=50_000, seed=9), cloud_radius=0.05)
+    _, cst, _ = scenes.make_constraint(robot, scene, self_collision=False)
+    _, oc, _ = oracle.make_constraint(robot, scene, self_collision=False)
+    Q = W.dualarm_configs(1024, seed=46)
+    ref = oc.is_valid(Q, threads=8)
+    assert 10 < ref.sum() < len(ref)  # 46 valid
+    plain = cst.is_valid_batch(Q)
+    assert np.array_equal(plain, ref)
+    assert np.array_equal(cst.is_valid_fast(Q), ref)
+    ok, d32 = cst.is_valid_fast(Q, distances=True)
+    assert np.array_equal(ok, ref)
+    d64 = np.minimum(cst.sphere_distances(Q[::4]), CUTOFF)
+    assert np.abs(d32[::4].astype(np.float64) - d64).max() < DIST_TOL
