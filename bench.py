@@ -610,19 +610,30 @@ def bench_single_calls(n: int = 2000):
         optr = C.c_void_p(ok.ctypes.data)
         ptrs = [C.c_void_p(qs[i].ctypes.data) for i in range(n)]
         got = np.empty(n, np.uint8)
-        for i in range(min(n, 50)):  # warm-up (tables, staging buffers)
-            lib.pmgpu_cst_is_valid(cst._h, ptrs[i], 1, optr, _lib.MEM_HOST, None)
-        t0 = time.perf_counter()
-        for i in range(n):
-            if lib.pmgpu_cst_is_valid(cst._h, ptrs[i], 1, optr, _lib.MEM_HOST, None) != 0:
-                raise RuntimeError(lib.pmgpu_last_error().decode())
-            got[i] = ok[0]
-        gpu_us = (time.perf_counter() - t0) / n * 1e6
+        got_f = np.empty(n, np.uint8)
+
+        def plain(i):
+            return lib.pmgpu_cst_is_valid(cst._h, ptrs[i], 1, optr, _lib.MEM_HOST, None)
+
+        def fast(i):
+            return lib.pmgpu_cst_is_valid_fast(cst._h, ptrs[i], 1, optr, None, None, _lib.MEM_HOST, None)
+
+        per_call = {}
+        for label, fn, dst in (("plain", plain, got), ("fast", fast, got_f)):
+            for i in range(min(n, 50)):  # warm-up (tables, staging buffers)
+                fn(i)
+            t0 = time.perf_counter()
+            for i in range(n):
+                if fn(i) != 0:
+                    raise RuntimeError(lib.pmgpu_last_error().decode())
+                dst[i] = ok[0]
+            per_call[label] = (time.perf_counter() - t0) / n * 1e6
         t0 = time.perf_counter()
         ref = oc.is_valid(qs, threads=1)
         cpu_us = (time.perf_counter() - t0) / n * 1e6
-        out[name] = {"is_valid_per_call_us": gpu_us, "oracle_single_core_us": cpu_us, "identical": bool(np.array_equal(got, ref)),
-                     "calls": n}
+        out[name] = {"is_valid_per_call_us": per_call["plain"], "is_valid_fast_per_call_us": per_call["fast"],
+                     "oracle_single_core_us": cpu_us,
+                     "identical": bool(np.array_equal(got, ref) and np.array_equal(got_f, ref)), "calls": n}
     # one edge at a time: checkMotion of the box validator (width 0.05) on the chain's edges
     robot, scene = W.chain7_robot(), W.chain7_scene()
     _, cst, _ = scenes.make_constraint(robot, scene)
@@ -634,23 +645,33 @@ def bench_single_calls(n: int = 2000):
     ok = np.zeros(1, np.uint8)
     optr = C.c_void_p(ok.ctypes.data)
     ne = s1.shape[0]
-    got = np.empty(ne, np.uint8)
-    for i in range(20):
-        lib.pmgpu_check_motion(cst._h, C.c_void_p(s1[i].ctypes.data), C.c_void_p(s2[i].ctypes.data), 1, 0, wptr, 0.0, optr, None,
-                               _lib.MEM_HOST, None)
     p1 = [C.c_void_p(s1[i].ctypes.data) for i in range(ne)]
     p2 = [C.c_void_p(s2[i].ctypes.data) for i in range(ne)]
-    t0 = time.perf_counter()
-    for i in range(ne):
-        if lib.pmgpu_check_motion(cst._h, p1[i], p2[i], 1, 0, wptr, 0.0, optr, None, _lib.MEM_HOST, None) != 0:
-            raise RuntimeError(lib.pmgpu_last_error().decode())
-        got[i] = ok[0]
-    gpu_us = (time.perf_counter() - t0) / ne * 1e6
+
+    def plain_e(i):
+        return lib.pmgpu_check_motion(cst._h, p1[i], p2[i], 1, 0, wptr, 0.0, optr, None, _lib.MEM_HOST, None)
+
+    def fast_e(i):
+        return lib.pmgpu_check_motion_fast(cst._h, p1[i], p2[i], 1, 0, wptr, 0.0, optr, None, _lib.MEM_HOST, None)
+
+    per_call, outs = {}, {}
+    for label, fn in (("plain", plain_e), ("fast", fast_e)):
+        got = np.empty(ne, np.uint8)
+        for i in range(20):
+            fn(i)
+        t0 = time.perf_counter()
+        for i in range(ne):
+            if fn(i) != 0:
+                raise RuntimeError(lib.pmgpu_last_error().decode())
+            got[i] = ok[0]
+        per_call[label] = (time.perf_counter() - t0) / ne * 1e6
+        outs[label] = got
     t0 = time.perf_counter()
     ref, _ = oc.check_motion(s1, s2, 0, width, threads=1)
     cpu_us = (time.perf_counter() - t0) / ne * 1e6
-    out["C1"] = {"check_motion_per_call_us": gpu_us, "oracle_single_core_us": cpu_us, "identical": bool(np.array_equal(got, ref)),
-                 "calls": ne}
+    out["C1"] = {"check_motion_per_call_us": per_call["plain"], "check_motion_fast_per_call_us": per_call["fast"],
+                 "oracle_single_core_us": cpu_us,
+                 "identical": bool(np.array_equal(outs["plain"], ref) and np.array_equal(outs["fast"], ref)), "calls": ne}
     out["what"] = ("per-call latency through the C ABI with host memory (one state / one edge per call, as OMPL's callbacks "
                    "call), against the oracle's single-core time per state / edge")
     return out

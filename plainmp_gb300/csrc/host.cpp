@@ -148,6 +148,30 @@ struct DevBuf {
   }
 };
 
+// Page-locked host buffer (grows, never shrinks): staging of small host-memory calls, so their
+// copies are plain DMA transfers on the stream instead of the driver's pageable-memory path.
+struct PinBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  PinBuf() = default;
+  PinBuf(const PinBuf&) = delete;
+  PinBuf& operator=(const PinBuf&) = delete;
+  ~PinBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  char* ensure(size_t bytes) {
+    if (bytes <= n && p) return static_cast<char*>(p);
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    const size_t b = std::max<size_t>(bytes, 4096);
+    cuda_check(cudaHostAlloc(&p, b, cudaHostAllocDefault), "cudaHostAlloc");
+    n = b;
+    return static_cast<char*>(p);
+  }
+};
+static size_t up16(size_t x) { return (x + 15) & ~(size_t)15; }
+
 // ---------------------------------------------------------------------------- host quaternion
 // construction-time helpers (setQuaternionFromRPY, transform.hpp:122-130)
 static void quat_from_rpy(double r, double p, double y, double q[4]) {
@@ -653,6 +677,7 @@ struct HostCst {
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
   DevBuf f_hq;                        // fast-path hard cloud queries (distances mode)
+  PinBuf h_pin;                       // pinned staging of small host-memory calls
   FastPipe pipe;                      // host-memory fast calls of large batches
   DevBuf e_sr, e_n, e_off;            // fast edge path: step ratios, waypoint counts and offsets
   DevBuf g_wp;                        // trajectory costs: per-waypoint partial costs
@@ -1837,24 +1862,38 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     const double* dq = q;
     uint8_t* dout = out;
     float* dd = dist32;
+    // host memory: one pinned staging buffer [q | out | dist | counters]
+    const size_t nq = (size_t)B * C.q_dim() * 8, nd = dist32 ? (size_t)B * C.n_spheres() * 4 : 0;
+    char* pin = nullptr;
     if (mem == PMGPU_MEM_HOST) {
-      dq = stage_in(C.w_in, q, (size_t)B * C.q_dim(), s);
+      pin = C.h_pin.ensure(up16(nq) + up16((size_t)B) + up16(nd) + 64);
+      std::memcpy(pin, q, nq);
+      double* dqw = (double*)C.w_in.ensure(std::max<size_t>(nq, 16));
+      if (nq) cuda_check(cudaMemcpyAsync(dqw, pin, nq, cudaMemcpyHostToDevice, s), "H2D copy");
+      dq = dqw;
       dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)B, 16));
-      dd = dist32 ? (float*)C.w_out2.ensure(std::max<size_t>((size_t)B * C.n_spheres() * 4, 16)) : nullptr;
+      dd = dist32 ? (float*)C.w_out2.ensure(std::max<size_t>(nd, 16)) : nullptr;
     }
     const unsigned hq_cap = hard_query_cap(B, C.n_spheres());
     void* hq = dd ? C.f_hq.ensure((size_t)hq_cap * 32) : nullptr;
     cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s, hq,
                                  (unsigned long long*)(ctl + 48), hq_cap),
                "is_valid_fast");
+    char* pin_out = pin ? pin + up16(nq) : nullptr;
+    char* pin_dist = pin ? pin_out + up16((size_t)B) : nullptr;
+    unsigned long long local_ctl[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long* h = pin ? reinterpret_cast<unsigned long long*>(pin_dist + up16(nd)) : local_ctl;
     if (mem == PMGPU_MEM_HOST) {
-      stage_out(out, dout, (size_t)B, s);
-      if (dist32) stage_out(dist32, dd, (size_t)B * C.n_spheres(), s);
+      if (B) cuda_check(cudaMemcpyAsync(pin_out, dout, (size_t)B, cudaMemcpyDeviceToHost, s), "D2H copy");
+      if (nd) cuda_check(cudaMemcpyAsync(pin_dist, dd, nd, cudaMemcpyDeviceToHost, s), "D2H copy");
     }
     if (stats || mem == PMGPU_MEM_HOST) {
-      unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
       cuda_check(cudaMemcpyAsync(h, ctl, 48, cudaMemcpyDeviceToHost, s), "D2H");
       cuda_check(cudaStreamSynchronize(s), "is_valid_fast");
+      if (mem == PMGPU_MEM_HOST) {
+        std::memcpy(out, pin_out, (size_t)B);
+        if (nd) std::memcpy(dist32, pin_dist, nd);
+      }
       if (stats) {
         stats[0] = B;
         stats[1] = (int64_t)(unsigned)h[0];
@@ -1933,12 +1972,24 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
     cudaStream_t s = as_stream(stream);
     const int16_t* seq = C.seq_table();
     const int d = C.q_dim();
+    const bool box = validator_type == PMGPU_VALIDATOR_BOX;
+    if (box) check_ptr(width, "width");
+    // host memory: one pinned staging buffer [s1 | s2 | width | out | counters]
+    const size_t ns_ = (size_t)E * d * 8, nw = box ? (size_t)d * 8 : 0;
+    char* pin = nullptr;
+    if (mem == PMGPU_MEM_HOST) {
+      pin = C.h_pin.ensure(2 * up16(ns_) + up16(nw) + up16((size_t)E) + 80);
+      std::memcpy(pin, s1, ns_);
+      std::memcpy(pin + up16(ns_), s2, ns_);
+      if (box) std::memcpy(pin + 2 * up16(ns_), width, nw);
+    }
     const double* dw = nullptr;
-    if (validator_type == PMGPU_VALIDATOR_BOX) {
-      check_ptr(width, "width");
+    if (box) {
       dw = (const double*)C.w_width.ensure((size_t)d * 8 + 16);
-      cuda_check(cudaMemcpyAsync((void*)dw, width, (size_t)d * 8, mem == PMGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
-                 "width");
+      if (mem == PMGPU_MEM_DEVICE)
+        cuda_check(cudaMemcpyAsync((void*)dw, width, nw, cudaMemcpyDeviceToDevice, s), "width");
+      else
+        cuda_check(cudaMemcpyAsync((void*)dw, pin + 2 * up16(ns_), nw, cudaMemcpyHostToDevice, s), "width");
     }
     const size_t En = (size_t)std::max<int64_t>(E, 1);
     double* sr = (double*)C.e_sr.ensure(En * 8);
@@ -1957,8 +2008,14 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
     const double* d2 = s2;
     uint8_t* dout = out;
     if (mem == PMGPU_MEM_HOST) {
-      d1 = stage_in(C.w_in, s1, (size_t)E * d, s);
-      d2 = stage_in(C.w_in2, s2, (size_t)E * d, s);
+      double* w1 = (double*)C.w_in.ensure(std::max<size_t>(ns_, 16));
+      double* w2 = (double*)C.w_in2.ensure(std::max<size_t>(ns_, 16));
+      if (ns_) {
+        cuda_check(cudaMemcpyAsync(w1, pin, ns_, cudaMemcpyHostToDevice, s), "H2D copy");
+        cuda_check(cudaMemcpyAsync(w2, pin + up16(ns_), ns_, cudaMemcpyHostToDevice, s), "H2D copy");
+      }
+      d1 = w1;
+      d2 = w2;
       dout = (uint8_t*)C.w_out.ensure(std::max<size_t>((size_t)E, 16));
     }
     int n_sm = 0;
@@ -1966,19 +2023,24 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
     cuda_check(launch_fast_edges(T, C.hdr, st, d1, d2, E, validator_type, dw, resolution, seq, sr, n, off, next, dout, items, count, cap,
                                  ovf, dstats, 32, n_sm, s),
                "check_motion_fast");
-    if (mem == PMGPU_MEM_HOST) stage_out(out, dout, (size_t)E, s);
+    char* pin_out = pin ? pin + 2 * up16(ns_) + up16(nw) : nullptr;
+    if (mem == PMGPU_MEM_HOST && E) cuda_check(cudaMemcpyAsync(pin_out, dout, (size_t)E, cudaMemcpyDeviceToHost, s), "D2H copy");
     if (stats || mem == PMGPU_MEM_HOST) {
-      unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
-      int64_t last_off = 0;
-      int32_t last_n = 0;
+      unsigned long long local_ctl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      unsigned long long* h = pin ? reinterpret_cast<unsigned long long*>(pin_out + up16((size_t)E)) : local_ctl;
+      int64_t* last_off = reinterpret_cast<int64_t*>(h + 6);
+      int32_t* last_n = reinterpret_cast<int32_t*>(h + 7);
+      *last_off = 0;
+      *last_n = 0;
       cuda_check(cudaMemcpyAsync(h, ctl, 48, cudaMemcpyDeviceToHost, s), "D2H");
-      if (E > 0) {
-        cuda_check(cudaMemcpyAsync(&last_off, off + E - 1, 8, cudaMemcpyDeviceToHost, s), "D2H");
-        cuda_check(cudaMemcpyAsync(&last_n, n + E - 1, 4, cudaMemcpyDeviceToHost, s), "D2H");
+      if (E > 0 && stats) {
+        cuda_check(cudaMemcpyAsync(last_off, off + E - 1, 8, cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaMemcpyAsync(last_n, n + E - 1, 4, cudaMemcpyDeviceToHost, s), "D2H");
       }
       cuda_check(cudaStreamSynchronize(s), "check_motion_fast");
+      if (mem == PMGPU_MEM_HOST) std::memcpy(out, pin_out, (size_t)E);
       if (stats) {
-        stats[0] = E > 0 ? last_off + last_n : 0;
+        stats[0] = E > 0 ? *last_off + *last_n : 0;
         stats[1] = (int64_t)(unsigned)h[0];
         stats[2] = (int64_t)h[4];
         stats[3] = 0;

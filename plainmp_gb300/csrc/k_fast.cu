@@ -22,6 +22,7 @@
 // also fails, so certain terms need no FP64 work.  Self pairs factor the same way.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -1712,11 +1713,29 @@ cudaError_t upload_offsets() {
   return e;
 }
 
+// The offset table on the device and the kernel's dynamic shared-memory limit raised to sm bytes;
+// both once per device (the attribute again only for a larger size), so small calls pay for neither.
 template <class K>
 static cudaError_t prep(K kern, size_t sm) {
   cudaError_t e = upload_offsets();
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int dev = 0;
+  if ((e = current_device(&dev)) != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> raised;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& have = raised[{reinterpret_cast<const void*>(kern), dev}];
+  if (have >= sm) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess) have = sm;
+  return e;
+}
+
+// Blocks of the recheck kernel: one 4-warp block per 32 configurations (or 8 edges), at most 4 per
+// SM; its loops stride over the grid, so a small batch launches few blocks.
+static unsigned recheck_grid(int64_t units, int per_block, int n_sm) {
+  const int64_t want = (units + per_block - 1) / per_block;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)n_sm * 4));
 }
 
 // count, overflow and stats must be zeroed by the caller
@@ -1764,7 +1783,7 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
     prof_end("k_hard_queries", s);
   }
   prof_begin("k_fast_recheck", s);
-  k_fast_recheck<CfgSource><<<n_sm * 4, 128, 0, s>>>(T, state, src, scr);
+  k_fast_recheck<CfgSource><<<recheck_grid(B, 32, n_sm), 128, 0, s>>>(T, state, src, scr);
   prof_end("k_fast_recheck", s);
   return cudaGetLastError();
 }
@@ -1789,13 +1808,15 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   int per_sm = 0;
   if ((e = prep(k_fast_edges<32, 128>, sm)) != cudaSuccess) return e;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<32, 128>, 128, sm)) != cudaSuccess) return e;
-  unsigned grid = (unsigned)(n_sm * (per_sm > 0 ? per_sm : 1));
+  // persistent blocks, at most 4 per edge (a few 32-waypoint chunks each): a small call stages the
+  // tables in few blocks
+  unsigned grid = (unsigned)std::min<int64_t>((int64_t)n_sm * (per_sm > 0 ? per_sm : 1), std::max<int64_t>(1, 4 * E));
   prof_begin("k_fast_edges", s);
   k_fast_edges<32, 128><<<grid, 128, sm, s>>>(T, state, src, next, scr);
   prof_end("k_fast_edges", s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_begin("k_fast_recheck_edges", s);
-  k_fast_recheck<EdgeSource><<<n_sm * 4, 128, 0, s>>>(T, state, src, scr);
+  k_fast_recheck<EdgeSource><<<recheck_grid(E, 8, n_sm), 128, 0, s>>>(T, state, src, scr);
   prof_end("k_fast_recheck_edges", s);
   return cudaGetLastError();
 }
