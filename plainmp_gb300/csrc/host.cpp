@@ -678,6 +678,7 @@ struct HostCst {
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
   DevBuf f_hq;                        // fast-path hard cloud queries (distances mode)
   PinBuf h_pin;                       // pinned staging of small host-memory calls
+  DevBuf w_cen;                       // sphere centres of a device-memory distances call without centres
   FastPipe pipe;                      // host-memory fast calls of large batches
   DevBuf e_sr, e_n, e_off;            // fast edge path: step ratios, waypoint counts and offsets
   DevBuf g_wp;                        // trajectory costs: per-waypoint partial costs
@@ -1710,13 +1711,15 @@ int pmgpu_cst_sphere_distances(pmgpu_cst* c, const double* q, int64_t B, int hig
     cudaStream_t s = as_stream(stream);
     int ns = C.n_spheres();
     if (mem == PMGPU_MEM_DEVICE) {
-      cuda_check(launch_sphere_dist64(T, st, q, B, high_accuracy, dist, centres, s), "sphere distances");
+      // the centres go to the caller's array, or to a workspace when only distances are wanted
+      double* dc = centres ? centres : (double*)C.w_cen.ensure(std::max<size_t>((size_t)B * ns * 24, 16));
+      cuda_check(launch_sphere_dist64(T, C.hdr, st, q, B, high_accuracy, dist, dc, s), "sphere distances");
       return;
     }
     const double* dq = stage_in(C.w_in, q, (size_t)B * C.q_dim(), s);
     double* dd = dist ? (double*)C.w_out.ensure(std::max<size_t>((size_t)B * ns * 8, 16)) : nullptr;
-    double* dc = centres ? (double*)C.w_out2.ensure(std::max<size_t>((size_t)B * ns * 24, 16)) : nullptr;
-    cuda_check(launch_sphere_dist64(T, st, dq, B, high_accuracy, dd, dc, s), "sphere distances");
+    double* dc = (double*)C.w_out2.ensure(std::max<size_t>((size_t)B * ns * 24, 16));
+    cuda_check(launch_sphere_dist64(T, C.hdr, st, dq, B, high_accuracy, dd, dc, s), "sphere distances");
     if (dist) stage_out(dist, dd, (size_t)B * ns, s);
     if (centres) stage_out(centres, dc, (size_t)B * ns * 3, s);
     cuda_check(cudaStreamSynchronize(s), "sphere distances");

@@ -203,8 +203,11 @@ __global__ void k_evaluate64(const PmTablesHdr* __restrict__ T, const double* __
   if (T->n_pairs > 0) vb[head] = eval_self(v, pose, jb + head * dof, jtmp, jtmp2);
 }
 
-__global__ void k_sphere_dist64(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, const double* __restrict__ q,
-                                int64_t B, int high_accuracy, double* __restrict__ dist, double* __restrict__ centres) {
+// Per-sphere signed distances in two launches: the FP64 sphere centres (one thread per configuration:
+// the FK), then the SDF of every (configuration, sphere) in its own thread, so the nearest-point
+// searches of a batch run side by side instead of one configuration's 120 in a row.
+__global__ void k_sphere_centres64(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, const double* __restrict__ q,
+                                   int64_t B, int high_accuracy, double* __restrict__ centres) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= B) return;
   TView v(T);
@@ -216,18 +219,22 @@ __global__ void k_sphere_dist64(const PmTablesHdr* __restrict__ T, const double*
     DM3 R = qmat(pose[g.slot].q);
     for (int k = g.begin; k < g.begin + g.count; k++) {
       D3 c = add(mv(R, v.rel(k)), pose[g.slot].t);
-      if (centres) {
-        centres[(b * ns + k) * 3 + 0] = c.x;
-        centres[(b * ns + k) * 3 + 1] = c.y;
-        centres[(b * ns + k) * 3 + 2] = c.z;
-      }
-      if (dist) {
-        double d = INFINITY;
-        for (int pi = 0; pi < T->n_prims; pi++) d = fmin(d, prim_eval(v.P[pi], v.C, c) - v.sr[k]);
-        dist[b * ns + k] = d;
-      }
+      centres[(b * ns + k) * 3 + 0] = c.x;
+      centres[(b * ns + k) * 3 + 1] = c.y;
+      centres[(b * ns + k) * 3 + 2] = c.z;
     }
   }
+}
+__global__ void k_sphere_sdf64(const PmTablesHdr* __restrict__ T, const double* __restrict__ centres, int64_t n,
+                               double* __restrict__ dist) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  TView v(T);
+  const int k = (int)(i % T->n_spheres);
+  const D3 c{centres[3 * i], centres[3 * i + 1], centres[3 * i + 2]};
+  double d = INFINITY;
+  for (int pi = 0; pi < T->n_prims; pi++) d = fmin(d, prim_eval(v.P[pi], v.C, c) - v.sr[k]);
+  dist[i] = d;
 }
 
 __global__ void k_spheres_of_state(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, int groups,
@@ -489,10 +496,14 @@ cudaError_t launch_evaluate64(const PmTablesHdr* T, const double* state, const d
   k_evaluate64<<<grid_for(B, 64), 64, 0, s>>>(T, state, q, B, high_accuracy, vals, jac);
   return cudaGetLastError();
 }
-cudaError_t launch_sphere_dist64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int high_accuracy,
-                                 double* dist, double* centres, cudaStream_t s) {
-  if (B <= 0) return cudaSuccess;
-  k_sphere_dist64<<<grid_for(B, 128), 128, 0, s>>>(T, state, q, B, high_accuracy, dist, centres);
+cudaError_t launch_sphere_dist64(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
+                                 int high_accuracy, double* dist, double* centres, cudaStream_t s) {
+  if (B <= 0 || h.n_spheres <= 0) return cudaSuccess;
+  k_sphere_centres64<<<grid_for(B, 128), 128, 0, s>>>(T, state, q, B, high_accuracy, centres);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !dist) return e;
+  const int64_t n = B * h.n_spheres;
+  k_sphere_sdf64<<<grid_for(n, 128), 128, 0, s>>>(T, centres, n, dist);
   return cudaGetLastError();
 }
 cudaError_t launch_spheres_of_state(const PmTablesHdr* T, const double* state, int groups, double* out4, cudaStream_t s) {

@@ -28,8 +28,9 @@ cudaError_t launch_is_valid64(const PmTablesHdr* T, const double* state, const d
                               cudaStream_t s);
 cudaError_t launch_evaluate64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int high_accuracy,
                               double* vals, double* jac, cudaStream_t s);
-cudaError_t launch_sphere_dist64(const PmTablesHdr* T, const double* state, const double* q, int64_t B, int high_accuracy,
-                                 double* dist, double* centres, cudaStream_t s);
+// centres (B x n_spheres x 3) is required: the distances are computed from it
+cudaError_t launch_sphere_dist64(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
+                                 int high_accuracy, double* dist, double* centres, cudaStream_t s);
 // spheres (all: groups=0, group spheres: groups=1) of the current state, out4 n x 4
 cudaError_t launch_spheres_of_state(const PmTablesHdr* T, const double* state, int groups, double* out4, cudaStream_t s);
 // checkMotion over E edges; seq: 128 x 128 int16 sequence table; width: q_dim (box) or NULL
