@@ -344,6 +344,7 @@ def bench_chain7(dev, timed):
                "deciles": [int(x) for x in np.percentile(wp, np.arange(10, 100, 10))]}
     S1, S2 = torch.tensor(s1, device=dev), torch.tensor(s2, device=dev)
     mv = BoxMotionValidator(cst, [0.05] * 7)
+    edge_shape, _ = autotune.autotune_edges(mv, S1, S2)
     ms_e_plain = timed(lambda: mv.check_motion_batch(S1, S2), 5)
     eout = torch.empty(S1.shape[0], dtype=torch.uint8, device=dev)
     ms_e_fast = timed(lambda: mv.check_motion_fast(S1, S2, out=eout), 10)
@@ -369,7 +370,8 @@ def bench_chain7(dev, timed):
                "unit": "edges/s", "plain_fp64": 1024 / (ms_e_plain / 1e3), "fast_persistent": 1024 / (ms_e_fast / 1e3),
                "fast_cuda_graph": 1024 / (ms_e_graph / 1e3) if ms_e_graph else None,
                "ms": {"plain_fp64": ms_e_plain, "fast_persistent": ms_e_fast, "fast_cuda_graph": ms_e_graph},
-               "edge_validity_identical": same_e, "waypoints_per_edge": wp_hist},
+               "edge_validity_identical": same_e, "waypoints_per_edge": wp_hist,
+               "edge_launch_shape": list(edge_shape)},
     }
 
 
@@ -811,9 +813,10 @@ def main():
 
     from plainmp_gb300 import autotune
 
-    shape_dist, _ = autotune.autotune(cst, Q, distances=True)
     shape_valid, _ = autotune.autotune(cst, Q, distances=False)
-    cst.set_fast_launch(*shape_dist)
+    tune_valid = cst.get_fast_tuning()
+    shape_dist, _ = autotune.autotune(cst, Q, distances=True)
+    tune_dist = cst.get_fast_tuning()
 
     def step():
         cst.is_valid_fast(Q, distances=True, out=out, dist_out=dout)
@@ -845,8 +848,9 @@ def main():
     k_ms, k_n = _lib.profile_read("k_fast_valid")
     h_ms, h_n = _lib.profile_read("k_hard_queries")
     r_ms, r_n = _lib.profile_read("k_fast_recheck")
+    f_ms, f_n = _lib.profile_read("k_fk32")
     rest_ms, rest_n = _lib.profile_read("*")
-    all_n = k_n + h_n + r_n + rest_n
+    all_n = k_n + h_n + r_n + f_n + rest_n
     total_ms = replicas.max_over_ranks(total_ms, dist, dev)
     ms_per_step = total_ms / args.steps
     value = world * B * args.steps / (total_ms / 1e3)
@@ -867,8 +871,10 @@ def main():
         return tt / n
 
     cst.set_fast_launch(*shape_valid)
+    cst.set_fast_tuning(*tune_valid)
     ms_valid = timed(lambda: cst.is_valid_fast(Q, out=out), 5)
     cst.set_fast_launch(*shape_dist)
+    cst.set_fast_tuning(*tune_dist)
     ms_plain = timed(lambda: cst.is_valid_batch(Q), 3)
     ok_fast = cst.is_valid_fast(Q).cpu().numpy()
     ok_plain = cst.is_valid_batch(Q).cpu().numpy()
@@ -956,14 +962,21 @@ def main():
         "dtype": "f32 (FP64 FK and FP64 recheck of uncertain decisions)",
         "data": "synthetic (seeded generators in plainmp_gb300/workloads.py)",
         "config": config_dict({"launch_shape": {"with_distances": list(shape_dist), "validity_only": list(shape_valid)},
+                               "autotuned": {
+                                   "with_distances": {"k_fast_valid": {"configs_per_block": shape_dist[0], "threads": shape_dist[1],
+                                                                       "sphere_tile": tune_dist[0]},
+                                                      "k_hard_queries": {"blocks_per_sm": tune_dist[1], "threads": 256}},
+                                   "validity_only": {"k_fast_valid": {"configs_per_block": shape_valid[0], "threads": shape_valid[1],
+                                                                      "sphere_tile": tune_valid[0]}},
+                                   "sphere_tile_0": "the least tile, 32 / configs_per_block spheres per warp row"},
                                "cloud_grid": sdf.stats()}),
         "e2e": {"value": e2e_value, "unit": "configs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": all_n,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": hbm_kind,
                      "kernel": "k_fast_valid + k_hard_queries", "kernel_ms": kernel_ms, "launches": k_n,
-                     "kernel_ms_each": {"k_fast_valid": k_ms / max(k_n, 1), "k_hard_queries": h_ms / max(h_n, 1),
-                                        "k_fast_recheck": r_ms / max(r_n, 1)},
+                     "kernel_ms_each": {"k_fk32": f_ms / max(f_n, 1), "k_fast_valid": k_ms / max(k_n, 1),
+                                        "k_hard_queries": h_ms / max(h_n, 1), "k_fast_recheck": r_ms / max(r_n, 1)},
                      "note": "HBM is not the binding resource: the kernel is issue/latency bound"
                              + (f" (ncu: SM issue active {issue} %, profiles/k_fast_valid_dualarm65536.md)" if issue else ""),
                      "issue": issue_step,

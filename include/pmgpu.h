@@ -189,6 +189,15 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
  * autotuner (plainmp_gb300/autotune.py).  No counterpart in the reference. */
 int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_per_block);
 int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* threads_per_block);
+/* The fast kernels' other tuning parameters, chosen per workload by the autotuner.  No counterpart
+ * in the reference.  sphere_tile: spheres of one configuration per warp row of sphere tasks (0 or a
+ * power of two up to 32; 0 and values below 32 / configurations-per-block give the least);
+ * hq_blocks_per_sm: blocks of 256 threads per SM of the hard cloud-query kernel (1..8);
+ * edge_configs_per_block, edge_threads: the edge kernel's waypoints and threads per block, one of
+ * (16,128) (32,128) (32,256) (64,256).  Defaults: 0, 4, 32, 128. */
+int pmgpu_cst_set_fast_tuning(pmgpu_cst* c, int sphere_tile, int hq_blocks_per_sm, int edge_configs_per_block, int edge_threads);
+int pmgpu_cst_get_fast_tuning(const pmgpu_cst* c, int* sphere_tile, int* hq_blocks_per_sm, int* edge_configs_per_block,
+                              int* edge_threads);
 
 /* Fast path for callers that must not allocate device memory during the call (real-time loops,
  * devices whose memory another allocator owns, code that cannot afford cudaMalloc's implicit

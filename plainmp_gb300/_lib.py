@@ -104,6 +104,8 @@ _SIGS = {
     "pmgpu_check_motion_fast": (_i, [_p, _p, _p, _i64, _i, _p, _d, _p, _p, _i, _p]),
     "pmgpu_cst_set_fast_launch": (_i, [_p, _i, _i]),
     "pmgpu_cst_get_fast_launch": (_i, [_p, C.POINTER(_i), C.POINTER(_i)]),
+    "pmgpu_cst_set_fast_tuning": (_i, [_p, _i, _i, _i, _i]),
+    "pmgpu_cst_get_fast_tuning": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
     "pmgpu_cst_link_poses": (_i, [_p, C.c_int32, _p, _i64, _p, _i, _p]),
     "pmgpu_linkpose_create": (_i, [_p, _cpp, _i, _i, _cpp, _i, _dp, _i32p, C.POINTER(_p)]),
     "pmgpu_linkbound_create": (_i, [_p, _cpp, _i, _i, C.c_char_p, _i, _i, _d, _i, _d, C.POINTER(_p)]),

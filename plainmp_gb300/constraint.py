@@ -198,6 +198,19 @@ class SphereCollisionCst(IneqConstraintBase):
         check(lib.pmgpu_cst_get_fast_launch(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_fast_tuning(self, sphere_tile: int = 0, hq_blocks_per_sm: int = 4, edge_configs_per_block: int = 32,
+                        edge_threads: int = 128) -> None:
+        """The fast kernels' other tuning parameters (see plainmp_gb300.autotune): spheres of one
+        configuration per warp row of sphere tasks (0: the least), blocks per SM of the hard
+        cloud-query kernel, and the edge kernel's waypoints and threads per block."""
+        check(lib.pmgpu_cst_set_fast_tuning(self._h, int(sphere_tile), int(hq_blocks_per_sm), int(edge_configs_per_block),
+                                             int(edge_threads)))
+
+    def get_fast_tuning(self) -> Tuple[int, int, int, int]:
+        v = [C.c_int() for _ in range(4)]
+        check(lib.pmgpu_cst_get_fast_tuning(self._h, *(C.byref(x) for x in v)))
+        return tuple(x.value for x in v)
+
     def is_valid_fast(self, Q, distances: bool = False, stats: bool = False, out=None, dist_out=None):
         """FP32 + FP64-recheck path: validity identical to is_valid_batch; optional FP32
         per-sphere signed distances clamped at the reference's 0.1 m cutoff (B, n_spheres) and

@@ -637,7 +637,7 @@ static std::vector<size_t> farthest_order(const std::vector<std::array<double, 3
 struct FastPipe {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  DevBuf in[2], out[2], dist[2], items[2], hq[2];
+  DevBuf in[2], out[2], dist[2], items[2], hq[2], pose[2];
   DevBuf ctl, ovf;  // per chunk counters (64 B each) and per-config overflow flags, for the whole call
   FastPipe() = default;
   FastPipe(const FastPipe&) = delete;
@@ -670,6 +670,8 @@ struct HostCst {
   PmTablesHdr hdr{};  // host copy of the device table header
   int fast_cpb = 32;  // configurations per block of the fast kernel
   int fast_nt = 256;  // threads per block of the fast kernel
+  FastTuning tune;    // the fast kernels' other autotuned parameters
+  int edge_cpb = 32, edge_nt = 128;  // waypoints and threads per block of the edge kernel
   std::vector<int> slot_of_link;
   std::vector<PmSlot> ctrl_recs;  // per control joint (child link, REV/PRIS) for state updates
   DevBuf d_ctrl_recs;
@@ -677,6 +679,7 @@ struct HostCst {
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
   DevBuf f_hq;                        // fast-path hard cloud queries (distances mode)
+  DevBuf f_pose;                      // fast-path FP32 poses of the FK kernel
   PinBuf h_pin;                       // pinned staging of small host-memory calls
   DevBuf w_cen;                       // sphere centres of a device-memory distances call without centres
   FastPipe pipe;                      // host-memory fast calls of large batches
@@ -1764,6 +1767,34 @@ int pmgpu_cst_set_fast_launch(pmgpu_cst* c, int configs_per_block, int threads_p
     c->c.fast_nt = threads_per_block;
   });
 }
+int pmgpu_cst_set_fast_tuning(pmgpu_cst* c, int sphere_tile, int hq_blocks_per_sm, int edge_configs_per_block, int edge_threads) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    int l = -1;
+    for (int k = 0; k <= 5; k++)
+      if (sphere_tile == (1 << k)) l = k;
+    if (sphere_tile != 0 && l < 0) throw std::invalid_argument("sphere_tile must be 0 or a power of two up to 32");
+    if (hq_blocks_per_sm < 1 || hq_blocks_per_sm > 8) throw std::invalid_argument("hq_blocks_per_sm must be in [1, 8]");
+    static const int ok[][2] = {{16, 128}, {32, 128}, {32, 256}, {64, 256}};
+    bool found = false;
+    for (auto& p : ok) found = found || (p[0] == edge_configs_per_block && p[1] == edge_threads);
+    if (!found) throw std::invalid_argument("unsupported edge (configs_per_block, threads_per_block) pair");
+    c->c.tune.sphere_tile_log2 = sphere_tile == 0 ? 0 : l;
+    c->c.tune.hq_blocks_per_sm = hq_blocks_per_sm;
+    c->c.edge_cpb = edge_configs_per_block;
+    c->c.edge_nt = edge_threads;
+  });
+}
+int pmgpu_cst_get_fast_tuning(const pmgpu_cst* c, int* sphere_tile, int* hq_blocks_per_sm, int* edge_configs_per_block,
+                              int* edge_threads) {
+  return guarded([&] {
+    check_ptr(c, "cst");
+    if (sphere_tile) *sphere_tile = c->c.tune.sphere_tile_log2 == 0 ? 0 : (1 << c->c.tune.sphere_tile_log2);
+    if (hq_blocks_per_sm) *hq_blocks_per_sm = c->c.tune.hq_blocks_per_sm;
+    if (edge_configs_per_block) *edge_configs_per_block = c->c.edge_cpb;
+    if (edge_threads) *edge_threads = c->c.edge_nt;
+  });
+}
 int pmgpu_cst_get_fast_launch(const pmgpu_cst* c, int* configs_per_block, int* threads_per_block) {
   return guarded([&] {
     check_ptr(c, "cst");
@@ -1795,9 +1826,11 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
   float* ddist[2];
   int4* items[2];
   void* hqb[2];
+  float* pose[2];
   const unsigned hq_cap = hard_query_cap(chunk, ns);
   for (int k = 0; k < 2; k++) {  // sized once per call, before any chunk is in flight
     hqb[k] = dist32 ? P.hq[k].ensure((size_t)hq_cap * 32) : nullptr;
+    pose[k] = (float*)P.pose[k].ensure((size_t)fast_pose_floats(C.hdr, chunk) * 4);
     din[k] = (double*)P.in[k].ensure((size_t)chunk * d * 8);
     dout[k] = (uint8_t*)P.out[k].ensure(std::max<size_t>((size_t)chunk, 16));
     ddist[k] = dist32 ? (float*)P.dist[k].ensure((size_t)chunk * ns * 4) : nullptr;
@@ -1816,7 +1849,8 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
     cuda_check(cudaMemcpyAsync(din[k], q + c0 * d, (size_t)(n * d) * 8, cudaMemcpyHostToDevice, cs), "H2D copy");
     char* cc = ctl + i * 64;
     cuda_check(launch_fast_valid(T, C.hdr, st, din[k], n, dout[k], ddist[k], 0.1f, items[k], (unsigned int*)cc, cap, ovf + c0,
-                                 (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs, hqb[k], (unsigned long long*)(cc + 48), hq_cap),
+                                 (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs, hqb[k], (unsigned long long*)(cc + 48), hq_cap,
+                                 pose[k], C.tune),
                "is_valid_fast");
     cuda_check(cudaMemcpyAsync(out + c0, dout[k], (size_t)n, cudaMemcpyDeviceToHost, cs), "D2H copy");
     if (dist32) cuda_check(cudaMemcpyAsync(dist32 + c0 * ns, ddist[k], (size_t)(n * ns) * 4, cudaMemcpyDeviceToHost, cs), "D2H copy");
@@ -1879,8 +1913,9 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     }
     const unsigned hq_cap = hard_query_cap(B, C.n_spheres());
     void* hq = dd ? C.f_hq.ensure((size_t)hq_cap * 32) : nullptr;
+    float* pose = (float*)C.f_pose.ensure(std::max<size_t>((size_t)fast_pose_floats(C.hdr, B) * 4, 16));
     cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s, hq,
-                                 (unsigned long long*)(ctl + 48), hq_cap),
+                                 (unsigned long long*)(ctl + 48), hq_cap, pose, C.tune),
                "is_valid_fast");
     char* pin_out = pin ? pin + up16(nq) : nullptr;
     char* pin_dist = pin ? pin_out + up16((size_t)B) : nullptr;
@@ -2024,7 +2059,7 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
     int n_sm = 0;
     cuda_check(sm_count(&n_sm), "device attribute");
     cuda_check(launch_fast_edges(T, C.hdr, st, d1, d2, E, validator_type, dw, resolution, seq, sr, n, off, next, dout, items, count, cap,
-                                 ovf, dstats, 32, n_sm, s),
+                                 ovf, dstats, C.edge_cpb, C.edge_nt, n_sm, s),
                "check_motion_fast");
     char* pin_out = pin ? pin + 2 * up16(ns_) + up16(nw) : nullptr;
     if (mem == PMGPU_MEM_HOST && E) cuda_check(cudaMemcpyAsync(pin_out, dout, (size_t)E, cudaMemcpyDeviceToHost, s), "D2H copy");

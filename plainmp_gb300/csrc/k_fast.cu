@@ -72,6 +72,7 @@ struct SlotF {
 // [18] eq = bound on |q - q64|_2.  A point s of the link frame then lies within et + eb |s| of
 // its FP64 position, plus the rounding of R s + t that margin32 covers.
 constexpr int kPoseF = 20;
+constexpr int kPoseUsed = 14;  // fields read after the FK: R, t, et, eb
 
 enum { ST_PASS = 0, ST_FAIL = 1, ST_MAYBE = 2 };
 constexpr int FLAG_FAIL = 1;
@@ -93,6 +94,10 @@ struct Scratch {
   HardQuery* hq;           // global hard-query queue (distances mode), or null: queries stay in the block
   unsigned long long* hq_count;  // entries reserved (64-bit: a large batch may reserve more than 2^32)
   unsigned int hq_cap;
+  const float* gpose;      // poses from k_fk32 ([slot][field][configuration], the batch's stride), or null:
+                           // each block runs the FK itself
+  int st_log2;             // sphere tile: log2 of the spheres a warp row of sphere tasks holds (0: the
+                           // least, 32 / configurations per block)
 };
 
 __device__ __forceinline__ float3 xf(const float* P, float x, float y, float z) {  // R (row-major 9) * v + t (P[9..11])
@@ -132,11 +137,13 @@ __device__ __forceinline__ void approx_sin_cos32(double x, float& s, float& c) {
 //     q -> R(q)v has derivative norm <= 6.4 |v| at |q| <= 1.001; matrix and product rounding);
 //   translation t = tp + R lt: |dt| <= |dtp| + (8 |dqp| + 24u)|lt| + 1.01 u (|tp|_1 + |lt|_1).
 // The base pose adds the rounding of q's base entries (and of their half angles).
-__device__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restrict__ base8, int base_type, int n_ctrl,
-                     const double* __restrict__ q, bool taylor, float* __restrict__ P) {
+// Field f of slot i is P[(i * kPoseF + f) * stride]: stride 1 in a block's shared memory, the batch
+// size in the FK kernel's [slot][field][configuration] layout.
+__device__ __forceinline__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restrict__ base8, int base_type, int n_ctrl,
+                                     const double* __restrict__ q, bool taylor, float* __restrict__ P, int64_t stride = 1) {
   for (int i = 0; i < nsl; i++) {
     const SlotF s = S[i];
-    float* o = P + i * kPoseF;
+    float* o = P + (int64_t)i * kPoseF * stride;
     FQ wq;
     float wt[3], eq, et;
     if (s.parent < 0) {
@@ -165,8 +172,8 @@ __device__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restri
       }
       et = kU * (fabsf(wt[0]) + fabsf(wt[1]) + fabsf(wt[2]));
     } else {
-      const float* pp = P + s.parent * kPoseF;
-      const FQ pq{pp[14], pp[15], pp[16], pp[17]};
+      const float* pp = P + (int64_t)s.parent * kPoseF * stride;
+      const FQ pq{pp[(14) * stride], pp[(15) * stride], pp[(16) * stride], pp[(17) * stride]};
       FQ lq{0.f, 0.f, 0.f, 1.f};
       float lt[3] = {s.lt[0], s.lt[1], s.lt[2]};
       float el = 0.f, elt = kU * s.lt1, lt1 = s.lt1;
@@ -195,23 +202,25 @@ __device__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restri
       }
       wq = lid ? pq : fqmul(pq, lq);
       for (int k = 0; k < 3; k++)
-        wt[k] = pp[9 + k] + fmaf(pp[3 * k], lt[0], fmaf(pp[3 * k + 1], lt[1], pp[3 * k + 2] * lt[2]));
-      const float peq = pp[18];
+        wt[k] = pp[(9 + k) * stride] + fmaf(pp[(3 * k) * stride], lt[0], fmaf(pp[(3 * k + 1) * stride], lt[1], pp[(3 * k + 2) * stride] * lt[2]));
+      const float peq = pp[(18) * stride];
       eq = lid ? peq + el : 1.001f * (peq + el) + 8.1f * kU;
       const float nlt = sqrtf(fmaf(lt[0], lt[0], fmaf(lt[1], lt[1], lt[2] * lt[2]))) * 1.001f;
-      et = pp[12] + nlt * pp[13] + 1.01f * kU * (fabsf(pp[9]) + fabsf(pp[10]) + fabsf(pp[11]) + lt1) + elt;
+      et = pp[(12) * stride] + nlt * pp[(13) * stride] + 1.01f * kU * (fabsf(pp[(9) * stride]) + fabsf(pp[(10) * stride]) + fabsf(pp[(11) * stride]) + lt1) + elt;
     }
-    fqmat(wq, o);
-    o[9] = wt[0];
-    o[10] = wt[1];
-    o[11] = wt[2];
-    o[12] = et;
-    o[13] = 8.0f * eq + 24.0f * kU;
-    o[14] = wq.x;
-    o[15] = wq.y;
-    o[16] = wq.z;
-    o[17] = wq.w;
-    o[18] = eq;
+    float R[9];
+    fqmat(wq, R);
+    for (int k = 0; k < 9; k++) o[k * stride] = R[k];
+    o[9 * stride] = wt[0];
+    o[10 * stride] = wt[1];
+    o[11 * stride] = wt[2];
+    o[12 * stride] = et;
+    o[13 * stride] = 8.0f * eq + 24.0f * kU;
+    o[14 * stride] = wq.x;
+    o[15 * stride] = wq.y;
+    o[16 * stride] = wq.z;
+    o[17 * stride] = wq.w;
+    o[18 * stride] = eq;
   }
 }
 
@@ -937,8 +946,35 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   const int ns = T->n_spheres, ng = T->n_groups, np = T->n_prims, npr = T->n_pairs, nsl = T->n_slots;
   const int tid = threadIdx.x;
   if (tid < CPB) sm.flags[tid] = 0;
-  // ---- 1. FK (FP32, with error bounds) -> shared memory
-  if (tid < ncfg) {
+  // ---- 1. FK (FP32, with error bounds) -> shared memory: from k_fk32's poses when it ran (the fields
+  //         the checks read: R, t and the two bounds), else here, one thread per configuration
+  if (scr.gpose != nullptr) {
+    const int64_t stride = src.n_overflow_slots();  // the batch size
+    const int total = CPB * nsl * kPoseUsed;
+    // 8 loads in flight per thread before their stores (a load waiting on the previous store would
+    // pay the memory latency once per element)
+    for (int base = tid; base < total; base += 8 * (int)blockDim.x) {
+      float val[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int idx = base + j * (int)blockDim.x;
+        const int c = idx & (CPB - 1), r = idx / CPB;  // configurations fastest: coalesced reads
+        const int f = r % kPoseUsed, i = r / kPoseUsed;
+        val[j] = idx < total && c < ncfg ? __ldg(scr.gpose + ((int64_t)i * kPoseF + f) * stride + c0 + c) : 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int idx = base + j * (int)blockDim.x;
+        const int c = idx & (CPB - 1), r = idx / CPB;
+        const int f = r % kPoseUsed, i = r / kPoseUsed;
+        if (idx < total && c < ncfg) sm.pose[((size_t)c * nsl + i) * kPoseF + f] = val[j];
+      }
+    }
+    if (tid < ncfg && scr.gpose[(int64_t)12 * stride + c0 + tid] < 0.f) {  // k_fk32's mark of a non-finite coordinate
+      sm.flags[tid] = 2;
+      scr.overflow[src.overflow_slot(c0 + tid)] = 1;
+    }
+  } else if (tid < ncfg) {
     if (src.pre_skip(c0 + tid)) {
       sm.flags[tid] = FLAG_FAIL | 2;  // already known invalid: no work
     } else {
@@ -990,9 +1026,15 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   }
   __syncthreads();
   const int hq_cap = T->n_clouds > 0 ? CPB * ns : 0;
-  // tasks are numbered with the configuration fastest (CPB is a power of two: no division), so
-  // neighbouring threads read the same sphere or pair records
-  const int n_sph_tasks = ns * CPB;
+  // Sphere tasks in warp rows of 32 / ST configurations (fastest) x ST spheres; ST = 2^stl is the
+  // sphere tile (autotuned), at least 32 / CPB so that a row holds every configuration once.  A small
+  // tile puts the same sphere on neighbouring lanes (shared records); a large one keeps a
+  // configuration's neighbouring spheres, and so their field cells, on one warp.  Pair tasks
+  // follow, numbered with the configuration fastest.  CPB is a power of two: no division.
+  constexpr int cpb_l = CPB == 16 ? 4 : (CPB == 32 ? 5 : (CPB == 64 ? 6 : 7));
+  const int stl = max(min(scr.st_log2, 5), cpb_l >= 5 ? 0 : 5 - cpb_l);
+  const int rl = 5 - stl, ncb_l = cpb_l - rl;  // configurations per row, rows per sphere tile (log2)
+  const int n_sph_tasks = (((ns + (1 << stl) - 1) >> stl) << ncb_l) << 5;
   const int n_tasks = n_sph_tasks + npr * CPB;
   const unsigned all_culled = np >= 32 ? 0xffffffffu : ((1u << np) - 1u);
   // one sphere of one configuration: primitives in-thread, cloud queries near the cloud queued
@@ -1063,7 +1105,10 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     const int t = t0 + lane;
     int hit_pi = -1, hit_c = 0;
     if (t < n_sph_tasks) {
-      sphere_task(t / CPB, t % CPB);
+      const int w = t >> 5, l = t & 31;
+      const int c = ((w & ((1 << ncb_l) - 1)) << rl) + (l & ((1 << rl) - 1));
+      const int si = ((w >> ncb_l) << stl) + (l >> rl);
+      if (si < ns) sphere_task(si, c);
     } else if (t < n_tasks) {
       const int u = t - n_sph_tasks;
       const int pi = u / CPB, c = u % CPB;
@@ -1292,7 +1337,9 @@ __device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
   return sm;
 }
 
-__device__ void stage_tables(const TView& v, const Smem& sm, const double* __restrict__ state) {
+// The FK slots (FP32, the local transforms' constant parts from the model state) and the fixed base
+// pose into shared memory (no barrier).
+__device__ void stage_slots(const TView& v, SlotF* __restrict__ slot, float* __restrict__ base8, const double* __restrict__ state) {
   const PmTablesHdr* T = v.T;
   const int tid = threadIdx.x;
   for (int i = tid; i < T->n_slots; i += blockDim.x) {
@@ -1315,12 +1362,18 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
     }
     for (int k = 0; k < 3; k++) f.lt[k] = (float)lt[k];
     f.lt1 = (float)((fabs(lt[0]) + fabs(lt[1]) + fabs(lt[2])) * (1.0 + 1e-6));
-    sm.slot[i] = f;
+    slot[i] = f;
   }
   if (tid < 8) {
     const double* b = state + (int64_t)PM_STATE_BASE_ROW * PM_STATE_STRIDE;
-    sm.base8[tid] = tid < 7 ? (float)b[tid] : 0.0f;
+    base8[tid] = tid < 7 ? (float)b[tid] : 0.0f;
   }
+}
+
+__device__ void stage_tables(const TView& v, const Smem& sm, const double* __restrict__ state) {
+  const PmTablesHdr* T = v.T;
+  const int tid = threadIdx.x;
+  stage_slots(v, sm.slot, sm.base8, state);
   for (int i = tid; i < T->n_spheres; i += blockDim.x) {
     SphereF s;
     s.x = (float)v.sx[i];
@@ -1370,6 +1423,30 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
   }
   for (int i = tid; i < T->n_pairs; i += blockDim.x) sm.pairs[i] = make_int2(v.pairs[2 * i], v.pairs[2 * i + 1]);
   __syncthreads();
+}
+
+// FP32 FK of a batch, one thread per configuration, the poses written in [slot][field][configuration]
+// order (the batch size as the stride) so that k_fast_valid's blocks read them coalesced; the parent
+// poses read back by the FK are the thread's own writes.  A configuration with a non-finite
+// coordinate gets et = -1 in slot 0 (a bound is never negative): k_fast_valid leaves it to the exact
+// FP64 check.
+__global__ void __launch_bounds__(128) k_fk32(const PmTablesHdr* __restrict__ T, const double* __restrict__ state,
+                                              const double* __restrict__ q, int64_t B, float* __restrict__ gpose) {
+  __shared__ SlotF s_slot[PM_MAX_SLOTS];
+  __shared__ float s_base8[8];
+  TView v(T);
+  stage_slots(v, s_slot, s_base8, state);
+  __syncthreads();
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const double* qc = q + b * T->q_dim;
+  bool finite = true;
+  for (int i = 0; i < T->q_dim; i++) finite = finite && isfinite(qc[i]);
+  if (finite) {
+    fk32(s_slot, T->n_slots, s_base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, gpose + b, B);
+  } else {
+    gpose[(int64_t)12 * B + b] = -1.0f;
+  }
 }
 
 // 64 registers a thread, stated as the occupancy target (NT threads x 65536 / (NT x 64) blocks
@@ -1432,18 +1509,23 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
   const int ns = T->n_spheres;
   const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t k = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
+  // each warp takes a contiguous range of the queue: queries pushed together (neighbouring spheres,
+  // the same block's configurations) then share the SM's L1
+  const int64_t per = (((n + 1) >> 1) + nw - 1) / nw * 2;  // queries per warp, even
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t k_end = min(n, (w + 1) * per);
+  int64_t k = w * per;  // the warp's pair: k (half 0), k + 1 (half 1)
   auto record = [&](int64_t i) {  // the half's query i
-    if (i >= n) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
+    if (i >= k_end) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
     const HardQuery h = hq[i];
     return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z, hl);
   };
   float4 rec = record(k + half);
-  while (k < n) {  // warp-uniform
-    const int64_t kn = k + 2 * nw;
+  while (k < k_end) {  // warp-uniform
+    const int64_t kn = k + 2;
     const float4 rec_n = record(kn + half);
     const int64_t i = k + half;
-    const bool have = i < n;  // the same on the half's lanes
+    const bool have = i < k_end;  // the same on the half's lanes
     HardQuery h;
     h.a = make_float4(0.f, 0.f, 0.f, 0.f);
     h.b = make_int4(0, 0, 0, 0);
@@ -1742,17 +1824,23 @@ static unsigned recheck_grid(int64_t units, int per_block, int n_sm) {
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq,
-                              unsigned long long* hq_count, unsigned int hq_cap) {
+                              unsigned long long* hq_count, unsigned int hq_cap, float* pose, const FastTuning& tune) {
   if (B <= 0) return cudaSuccess;
   if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   // (hard-query entries hold 32-bit configuration indices)
   const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
-              split ? hq_cap : 0u};
+              split ? hq_cap : 0u, pose, tune.sphere_tile_log2};
   size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
   cudaError_t e;
+  if (pose) {
+    prof_begin("k_fk32", s);
+    k_fk32<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(T, state, q, B, pose);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_end("k_fk32", s);
+  }
   prof_begin("k_fast_valid", s);
 #define PM_FAST_CASE(C, N)                                                                      \
   if (cpb == C && nt == N) {                                                                     \
@@ -1778,7 +1866,8 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if ((e = sm_count(&n_sm)) != cudaSuccess) return e;
   if (split) {
     prof_begin("k_hard_queries", s);
-    k_hard_queries<CfgSource><<<n_sm * 4, 256, 0, s>>>(T, scr.hq, dist32, src, scr);
+    const int bps = tune.hq_blocks_per_sm >= 1 && tune.hq_blocks_per_sm <= 8 ? tune.hq_blocks_per_sm : 4;
+    k_hard_queries<CfgSource><<<n_sm * bps, 256, 0, s>>>(T, scr.hq, dist32, src, scr);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_end("k_hard_queries", s);
   }
@@ -1793,7 +1882,7 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
 cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
                               int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,
                               int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
-                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int n_sm, cudaStream_t s) {
+                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int nt, int n_sm, cudaStream_t s) {
   if (E <= 0) return cudaSuccess;
   if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   Scratch scr{items, count, cap, overflow, stats};
@@ -1805,15 +1894,26 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   EdgeSource src{s1, s2, off, n, sr, seq, E, out};
   size_t sm = fast_smem_bytes(h, cpb, false);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
-  int per_sm = 0;
-  if ((e = prep(k_fast_edges<32, 128>, sm)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<32, 128>, 128, sm)) != cudaSuccess) return e;
-  // persistent blocks, at most 4 per edge (a few 32-waypoint chunks each): a small call stages the
+  bool launched = false;
+  // persistent blocks, at most 4 per edge (a few chunks of waypoints each): a small call stages the
   // tables in few blocks
-  unsigned grid = (unsigned)std::min<int64_t>((int64_t)n_sm * (per_sm > 0 ? per_sm : 1), std::max<int64_t>(1, 4 * E));
-  prof_begin("k_fast_edges", s);
-  k_fast_edges<32, 128><<<grid, 128, sm, s>>>(T, state, src, next, scr);
-  prof_end("k_fast_edges", s);
+#define PM_EDGE_CASE(C, N)                                                                                               \
+  if (cpb == C && nt == N) {                                                                                              \
+    int per_sm = 0;                                                                                                      \
+    if ((e = prep(k_fast_edges<C, N>, sm)) != cudaSuccess) return e;                                                      \
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast_edges<C, N>, N, sm)) != cudaSuccess) return e; \
+    const unsigned grid = (unsigned)std::min<int64_t>((int64_t)n_sm * (per_sm > 0 ? per_sm : 1), std::max<int64_t>(1, 4 * E)); \
+    prof_begin("k_fast_edges", s);                                                                                        \
+    k_fast_edges<C, N><<<grid, N, sm, s>>>(T, state, src, next, scr);                                                     \
+    prof_end("k_fast_edges", s);                                                                                          \
+    launched = true;                                                                                                     \
+  }
+  PM_EDGE_CASE(16, 128)
+  PM_EDGE_CASE(32, 128)
+  PM_EDGE_CASE(32, 256)
+  PM_EDGE_CASE(64, 256)
+#undef PM_EDGE_CASE
+  if (!launched) return cudaErrorInvalidValue;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_begin("k_fast_recheck_edges", s);
   k_fast_recheck<EdgeSource><<<recheck_grid(E, 8, n_sm), 128, 0, s>>>(T, state, src, scr);

@@ -257,33 +257,56 @@ def test_fast_edges_degenerate(chain):
 
 
 def test_fast_every_launch_shape(dual):
-    """Every (configs per block, threads) pair the autotuner may pick gives the same validity and
-    the same FP32 distances: the shape changes the work split, never the arithmetic."""
+    """Every (configs per block, threads) pair and sphere tile the autotuner may pick, and every
+    hard-query grid, gives the same validity and the same FP32 distances (validity-only and with
+    distances): the tuning changes the work split, never the arithmetic."""
     from plainmp_gb300._lib import CudaError
-    from plainmp_gb300.autotune import SHAPES
+    from plainmp_gb300.autotune import SHAPES, sphere_tiles
 
     (_, cst, _), (_, oc, _) = dual
     Q = W.dualarm_configs(777, seed=21)  # a ragged last block for every shape
     ref = oc.is_valid(Q, threads=8)
-    keep = cst.get_fast_launch()
+    keep, keep_t = cst.get_fast_launch(), cst.get_fast_tuning()
     ran = 0
     try:
         d0 = None
         for cpb, nt in SHAPES:
             cst.set_fast_launch(cpb, nt)
-            try:
-                ok, d = cst.is_valid_fast(Q, distances=True)
-            except CudaError as e:  # the block's tables do not fit in shared memory at this shape
-                assert "invalid configuration" in str(e), (cpb, nt, str(e))
-                continue
-            ran += 1
-            assert np.array_equal(ok, ref), (cpb, nt)
-            if d0 is None:
-                d0 = d
-            assert np.array_equal(d, d0), (cpb, nt)
+            for st in sphere_tiles(cpb):
+                cst.set_fast_tuning(st, 2 + ran % 3, 32, 128)
+                try:
+                    ok, d = cst.is_valid_fast(Q, distances=True)
+                except CudaError as e:  # the block's tables do not fit in shared memory at this shape
+                    assert "invalid configuration" in str(e), (cpb, nt, str(e))
+                    break
+                ran += 1
+                assert np.array_equal(ok, ref), (cpb, nt, st)
+                assert np.array_equal(cst.is_valid_fast(Q), ref), (cpb, nt, st)
+                if d0 is None:
+                    d0 = d
+                assert np.array_equal(d, d0), (cpb, nt, st)
     finally:
         cst.set_fast_launch(*keep)
-    assert ran >= 5, ran
+        cst.set_fast_tuning(*keep_t)
+    assert ran >= 20, ran
+
+
+def test_fast_edges_every_launch_shape(chain):
+    """Every edge-kernel launch shape the autotuner may pick gives the oracle's edge booleans."""
+    from plainmp_gb300.autotune import EDGE_SHAPES
+
+    (_, cst, _), (_, oc, _) = chain
+    s1, s2 = W.chain7_edges(300, seed=23)
+    w = np.full(7, 0.05)
+    ref, _ = oc.check_motion(s1, s2, 0, w, threads=8)
+    mv = BoxMotionValidator(cst, w)
+    keep = cst.get_fast_tuning()
+    try:
+        for ecpb, ent in EDGE_SHAPES:
+            cst.set_fast_tuning(keep[0], keep[1], ecpb, ent)
+            assert np.array_equal(mv.check_motion_fast(s1, s2), ref), (ecpb, ent)
+    finally:
+        cst.set_fast_tuning(*keep)
 
 
 def test_fma_peak_microbenchmark():

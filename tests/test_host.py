@@ -556,3 +556,19 @@ def test_bench_traj_cost_check(monkeypatch):
     monkeypatch.setattr(diff, "traj_cost_grad", fake_cost)
     r = bench.traj_cost_check(FakeCst(), q32, off)
     assert r["trajectories"] == 16 and 0 <= r["max_rel_err"] < 1e-6  # FP32 rounding of the cost only
+
+
+def test_fast_tuning_arguments():
+    """The fast kernels' tuning parameters (the autotuner's sphere tile, hard-query grid and edge
+    shape): defaults, a round trip and the refusals of unsupported values, all on the host."""
+    from plainmp_gb300 import scenes
+    from plainmp_gb300 import workloads as W
+
+    _, cst, _ = scenes.make_constraint(W.chain7_robot(), W.chain7_scene())
+    assert cst.get_fast_tuning() == (0, 4, 32, 128)
+    cst.set_fast_tuning(8, 2, 64, 256)
+    assert cst.get_fast_tuning() == (8, 2, 64, 256)
+    for bad in ((3, 4, 32, 128), (64, 4, 32, 128), (0, 0, 32, 128), (0, 9, 32, 128), (0, 4, 8, 64), (0, 4, 32, 512)):
+        with pytest.raises(ValueError):
+            cst.set_fast_tuning(*bad)
+    assert cst.get_fast_tuning() == (8, 2, 64, 256)
