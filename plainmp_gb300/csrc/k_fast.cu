@@ -850,16 +850,11 @@ __device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int6
   }
 }
 
-// Room of a block's hard-query queue: half of its (configuration, sphere) tasks (the dual-arm cloud
-// batch queues about 6 %); a block whose queries do not fit answers the rest in the sphere task.
-__host__ __device__ inline int hq_capacity(const PmTablesHdr& h, int cpb) { return h.n_clouds > 0 ? (cpb * h.n_spheres + 1) / 2 : 0; }
-
 struct Smem {
   double* qbuf;  // generated configurations (edges)
   int2* hq;      // hard cloud queries: (cfg << 16 | sphere, primitive)
   int* hq_n;     // [0] pushed, [1] popped
   int* sdist;    // per (cfg, sphere): running minimum signed distance, order-preserving int
-  float* fld;    // per (cfg, sphere): the first cloud's field bound at the sphere centre (+inf: none)
   float* pose;   // [cfg][slot][kPoseF]
   SlotF* slot;
   float* base8;  // fixed base pose: q xyzw, t xyz
@@ -1022,40 +1017,6 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     }
     sm.cull[c * ng + gi] = mask;
   }
-  // ---- 2b. the first cloud's field bound at every sphere centre, into shared memory; its loads go
-  //          out four at a time per thread, so a block pays the memory latency once, not once per task
-  const int pc = sm.hq_n[3];  // the first cloud primitive (-1: none), from the staging
-  constexpr int cpb_l = CPB == 16 ? 4 : (CPB == 32 ? 5 : (CPB == 64 ? 6 : 7));
-  if (pc >= 0) {  // block-uniform
-    const PmGridDev& Gc = v.C[sm.prm[pc].cloud];
-    const int total = CPB * ns;
-    for (int base = tid; base < total; base += 4 * (int)blockDim.x) {
-      int2 raw[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int idx = base + j * (int)blockDim.x;
-        const int c = idx & (CPB - 1), si = idx >> cpb_l;
-        raw[j] = make_int2(__float_as_int(INFINITY), -1);
-        if (idx < total && c < ncfg && !(sm.flags[c] & 2)) {
-          const SphereF S = sm.sph[si];
-          const float* P = sm.pose + ((size_t)c * nsl + sm.grp[S.group].slot) * kPoseF;
-          const float3 sc = xf(P, S.x, S.y, S.z);
-          raw[j] = grid_field_nn32(Gc, sc.x, sc.y, sc.z);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int idx = base + j * (int)blockDim.x;
-        const int c = idx & (CPB - 1), si = idx >> cpb_l;
-        if (idx < total && c < ncfg && !(sm.flags[c] & 2)) {
-          const SphereF S = sm.sph[si];
-          const float* P = sm.pose + ((size_t)c * nsl + sm.grp[S.group].slot) * kPoseF;
-          const float3 sc = xf(P, S.x, S.y, S.z);  // as above
-          sm.fld[c * ns + si] = grid_field_lb32(Gc, sc.x, sc.y, sc.z, raw[j]);
-        }
-      }
-    }
-  }
   __syncthreads();
   // ---- 3a. sphere tasks (primitives in-thread; cloud queries near the cloud are queued) and
   //          self-pair tasks
@@ -1064,12 +1025,13 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     sm.hq_n[1] = 0;
   }
   __syncthreads();
-  const int hq_cap = hq_capacity(*T, CPB);
+  const int hq_cap = T->n_clouds > 0 ? CPB * ns : 0;
   // Sphere tasks in warp rows of 32 / ST configurations (fastest) x ST spheres; ST = 2^stl is the
   // sphere tile (autotuned), at least 32 / CPB so that a row holds every configuration once.  A small
   // tile puts the same sphere on neighbouring lanes (shared records); a large one keeps a
   // configuration's neighbouring spheres, and so their field cells, on one warp.  Pair tasks
   // follow, numbered with the configuration fastest.  CPB is a power of two: no division.
+  constexpr int cpb_l = CPB == 16 ? 4 : (CPB == 32 ? 5 : (CPB == 64 ? 6 : 7));
   const int stl = max(min(scr.st_log2, 5), cpb_l >= 5 ? 0 : 5 - cpb_l);
   const int rl = 5 - stl, ncb_l = cpb_l - rl;  // configurations per row, rows per sphere tile (log2)
   const int n_sph_tasks = (((ns + (1 << stl) - 1) >> stl) << ncb_l) << 5;
@@ -1099,14 +1061,9 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       float g, sd, mag;
       if (Pr.kind == PM_SDF_CLOUD) {
         const PmGridDev& Gc = v.C[Pr.cloud];
-        // the first cloud's bound is in shared memory (2b); the nearest point of the field, which
-        // only the validity-only shortcut below reads, is loaded when that shortcut is reached
-        FieldLB fb{INFINITY, -1, make_float4(0.f, 0.f, 0.f, 0.f)};
-        if (p == pc) fb.lb = sm.fld[c * ns + si];
-        else fb = grid_field32(Gc, sc.x, sc.y, sc.z, !want_dist && check);
+        const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z, !want_dist && check);
         const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
         if (fb.lb - Pr.a - S.r > margin32(qmag + fb.lb) + ek + (want_dist ? cutoff : 0.f)) continue;
-        if (!want_dist && check && p == pc) fb = grid_field32(Gc, sc.x, sc.y, sc.z, true);
         if (!want_dist && check && fb.idx >= 0) {
           // the centre's nearest point is a real point: if it is certainly within reach, the
           // sphere collides and no search is needed
@@ -1325,11 +1282,10 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
 
 // Shared-memory layout of a fast block; every array starts on a 16-byte boundary.
 struct SmemLayout {
-  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, hq_n, hq, fld, sdist, total;
+  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, hq_n, hq, sdist, total;
 };
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
-// gen: the configurations are generated in the block (edges), which needs qbuf.
-__host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb, bool want_dist, bool gen) {
+__host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb, bool want_dist) {
   SmemLayout L;
   size_t o = 0;
   L.pose = o;
@@ -1351,21 +1307,19 @@ __host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb,
   L.cull = o;
   o = a16(o + sizeof(unsigned) * (size_t)cpb * h.n_groups);
   L.qbuf = o;
-  o = a16(o + (gen ? sizeof(double) * (size_t)cpb * h.q_dim : 0));
+  o = a16(o + sizeof(double) * (size_t)cpb * h.q_dim);
   L.hq_n = o;
   o = a16(o + 16);
   L.hq = o;
-  o = a16(o + sizeof(int2) * (size_t)hq_capacity(h, cpb));
-  L.fld = o;
-  o = a16(o + (h.n_clouds > 0 ? sizeof(float) * (size_t)cpb * h.n_spheres : 0));
+  o = a16(o + (h.n_clouds > 0 ? sizeof(int2) * (size_t)cpb * h.n_spheres : 0));
   L.sdist = o;
   o = a16(o + (want_dist ? sizeof(int) * (size_t)cpb * h.n_spheres : 0));
   L.total = o;
   return L;
 }
 
-__device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb, bool gen) {
-  const SmemLayout L = smem_layout(*T, cpb, true, gen);
+__device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
+  const SmemLayout L = smem_layout(*T, cpb, true);
   Smem sm;
   sm.pose = reinterpret_cast<float*>(p + L.pose);
   sm.slot = reinterpret_cast<SlotF*>(p + L.slot);
@@ -1379,7 +1333,6 @@ __device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb, bool gen)
   sm.qbuf = reinterpret_cast<double*>(p + L.qbuf);
   sm.hq_n = reinterpret_cast<int*>(p + L.hq_n);
   sm.hq = reinterpret_cast<int2*>(p + L.hq);        // only with a point cloud
-  sm.fld = reinterpret_cast<float*>(p + L.fld);     // only with a point cloud
   sm.sdist = reinterpret_cast<int*>(p + L.sdist);   // only with distance output (the last array)
   return sm;
 }
@@ -1469,45 +1422,32 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
     sm.prm[i] = f;
   }
   for (int i = tid; i < T->n_pairs; i += blockDim.x) sm.pairs[i] = make_int2(v.pairs[2 * i], v.pairs[2 * i + 1]);
-  if (tid == 0) {
-    int pc = -1;
-    for (int i = 0; i < T->n_prims && pc < 0; i++)
-      if (v.P[i].kind == PM_SDF_CLOUD) pc = i;
-    sm.hq_n[3] = pc;
-  }
   __syncthreads();
 }
 
-// FP32 FK of a batch, one thread per configuration: the FK runs in the thread's own region of shared
-// memory (kPoseF floats per slot), then the fields the checks read go out in
-// [slot][field][configuration] order (the batch size as the stride), coalesced, for k_fast_valid's
-// blocks to read the same way.  A configuration with a non-finite coordinate gets et = -1 in slot 0
-// (a bound is never negative): k_fast_valid leaves it to the exact FP64 check.
-__global__ void k_fk32(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, const double* __restrict__ q, int64_t B,
-                       float* __restrict__ gpose) {
-  extern __shared__ __align__(16) unsigned char fk_smem[];
-  SlotF* s_slot = reinterpret_cast<SlotF*>(fk_smem);
-  float* s_base8 = reinterpret_cast<float*>(fk_smem + sizeof(SlotF) * PM_MAX_SLOTS);
-  float* s_pose = s_base8 + 8;
+// FP32 FK of a batch, one thread per configuration, the poses written in [slot][field][configuration]
+// order (the batch size as the stride) so that k_fast_valid's blocks read them coalesced; the parent
+// poses read back by the FK are the thread's own writes.  A configuration with a non-finite
+// coordinate gets et = -1 in slot 0 (a bound is never negative): k_fast_valid leaves it to the exact
+// FP64 check.
+__global__ void __launch_bounds__(128) k_fk32(const PmTablesHdr* __restrict__ T, const double* __restrict__ state,
+                                              const double* __restrict__ q, int64_t B, float* __restrict__ gpose) {
+  __shared__ SlotF s_slot[PM_MAX_SLOTS];
+  __shared__ float s_base8[8];
   TView v(T);
   stage_slots(v, s_slot, s_base8, state);
   __syncthreads();
-  const int nsl = T->n_slots;
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= B) return;
   const double* qc = q + b * T->q_dim;
   bool finite = true;
   for (int i = 0; i < T->q_dim; i++) finite = finite && isfinite(qc[i]);
-  if (!finite) {
+  if (finite) {
+    fk32(s_slot, T->n_slots, s_base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, gpose + b, B);
+  } else {
     gpose[(int64_t)12 * B + b] = -1.0f;
-    return;
   }
-  float* P = s_pose + (size_t)threadIdx.x * nsl * kPoseF;
-  fk32(s_slot, nsl, s_base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, P);
-  for (int i = 0; i < nsl; i++)
-    for (int f = 0; f < kPoseUsed; f++) gpose[((int64_t)i * kPoseF + f) * B + b] = P[i * kPoseF + f];
 }
-size_t fk32_smem(int nsl, int threads) { return sizeof(SlotF) * PM_MAX_SLOTS + 32 + sizeof(float) * kPoseF * (size_t)nsl * threads; }
 
 // 64 registers a thread, stated as the occupancy target (NT threads x 65536 / (NT x 64) blocks
 // per SM): the same budget the compiler picks for NT alone, but its allocation under the explicit
@@ -1518,7 +1458,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 64)) k_fast_valid(const PmTa
                                                     float* __restrict__ dist32, float cutoff, Scratch scr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TView v(T);
-  Smem sm = carve(smem_raw, T, CPB, false);
+  Smem sm = carve(smem_raw, T, CPB);
   stage_tables(v, sm, state);
   CfgSource src{q, B, out};
   const int64_t c0 = (int64_t)blockIdx.x * CPB;
@@ -1534,7 +1474,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 64)) k_fast_edges(const PmTa
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long long chunk;
   TView v(T);
-  Smem sm = carve(smem_raw, T, CPB, true);
+  Smem sm = carve(smem_raw, T, CPB);
   stage_tables(v, sm, state);
   const int64_t W = src.E > 0 ? src.off[src.E - 1] + src.n[src.E - 1] : 0;
   for (;;) {
@@ -1569,18 +1509,23 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
   const int ns = T->n_spheres;
   const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t k = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
+  // each warp takes a contiguous range of the queue: queries pushed together (neighbouring spheres,
+  // the same block's configurations) then share the SM's L1
+  const int64_t per = (((n + 1) >> 1) + nw - 1) / nw * 2;  // queries per warp, even
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t k_end = min(n, (w + 1) * per);
+  int64_t k = w * per;  // the warp's pair: k (half 0), k + 1 (half 1)
   auto record = [&](int64_t i) {  // the half's query i
-    if (i >= n) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
+    if (i >= k_end) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
     const HardQuery h = hq[i];
     return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z, hl);
   };
   float4 rec = record(k + half);
-  while (k < n) {  // warp-uniform
-    const int64_t kn = k + 2 * nw;
+  while (k < k_end) {  // warp-uniform
+    const int64_t kn = k + 2;
     const float4 rec_n = record(kn + half);
     const int64_t i = k + half;
-    const bool have = i < n;  // the same on the half's lanes
+    const bool have = i < k_end;  // the same on the half's lanes
     HardQuery h;
     h.a = make_float4(0.f, 0.f, 0.f, 0.f);
     h.b = make_int4(0, 0, 0, 0);
@@ -1781,7 +1726,7 @@ __global__ void k_scan1(const int32_t* __restrict__ n, int64_t E, int64_t* __res
 
 namespace pmg {
 
-size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist, bool gen) { return smem_layout(h, cpb, want_dist, gen).total; }
+size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist) { return smem_layout(h, cpb, want_dist).total; }
 
 // Queue records pack a sphere index in 16 bits and a primitive index in 15 (HardQuery.b.y: sphere |
 // primitive << 16 | check << 31; the block's queue: configuration << 16 | sphere).  The tables of
@@ -1886,17 +1831,13 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
               split ? hq_cap : 0u, pose, tune.sphere_tile_log2};
-  size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr, false);
+  size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
   cudaError_t e;
   if (pose) {
-    // threads per block: the most (up to 128, a multiple of 32) whose FK regions fit in 48 KB
-    const int fk_nt = std::max(32, std::min(128, (int)((48 * 1024 - sizeof(SlotF) * PM_MAX_SLOTS - 32) / (sizeof(float) * kPoseF * h.n_slots)) / 32 * 32));
-    const size_t fk_sm = fk32_smem(h.n_slots, fk_nt);
-    if ((e = prep(k_fk32, fk_sm)) != cudaSuccess) return e;
     prof_begin("k_fk32", s);
-    k_fk32<<<(unsigned)((B + fk_nt - 1) / fk_nt), fk_nt, fk_sm, s>>>(T, state, q, B, pose);
+    k_fk32<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(T, state, q, B, pose);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_end("k_fk32", s);
   }
@@ -1951,7 +1892,7 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   k_scan1<<<1, 1024, 0, s>>>(n, E, off);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   EdgeSource src{s1, s2, off, n, sr, seq, E, out};
-  size_t sm = fast_smem_bytes(h, cpb, false, true);
+  size_t sm = fast_smem_bytes(h, cpb, false);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   bool launched = false;
   // persistent blocks, at most 4 per edge (a few chunks of waypoints each): a small call stages the

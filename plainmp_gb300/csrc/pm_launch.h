@@ -39,7 +39,7 @@ cudaError_t launch_check_motion64(const PmTablesHdr* T, const double* state, con
                                   unsigned long long* n_checked, cudaStream_t s);
 
 // ---- fast path (k_fast.cu): FP32 decisions + FP64 recheck of uncertain terms.
-size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist, bool gen = false);
+size_t fast_smem_bytes(const PmTablesHdr& h, int cpb, bool want_dist);
 // The fast kernels' queue records hold at most 65,535 spheres and 32,767 primitives.
 bool fast_table_sizes_ok(const PmTablesHdr& h);
 // SM count of the current device (cached per device); the offset table of the warp searches,
