@@ -848,9 +848,8 @@ def main():
     k_ms, k_n = _lib.profile_read("k_fast_valid")
     h_ms, h_n = _lib.profile_read("k_hard_queries")
     r_ms, r_n = _lib.profile_read("k_fast_recheck")
-    f_ms, f_n = _lib.profile_read("k_fk32")
     rest_ms, rest_n = _lib.profile_read("*")
-    all_n = k_n + h_n + r_n + f_n + rest_n
+    all_n = k_n + h_n + r_n + rest_n
     total_ms = replicas.max_over_ranks(total_ms, dist, dev)
     ms_per_step = total_ms / args.steps
     value = world * B * args.steps / (total_ms / 1e3)
@@ -975,8 +974,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": hbm_kind,
                      "kernel": "k_fast_valid + k_hard_queries", "kernel_ms": kernel_ms, "launches": k_n,
-                     "kernel_ms_each": {"k_fk32": f_ms / max(f_n, 1), "k_fast_valid": k_ms / max(k_n, 1),
-                                        "k_hard_queries": h_ms / max(h_n, 1), "k_fast_recheck": r_ms / max(r_n, 1)},
+                     "kernel_ms_each": {"k_fast_valid": k_ms / max(k_n, 1), "k_hard_queries": h_ms / max(h_n, 1),
+                                        "k_fast_recheck": r_ms / max(r_n, 1)},
                      "note": "HBM is not the binding resource: the kernel is issue/latency bound"
                              + (f" (ncu: SM issue active {issue} %, profiles/k_fast_valid_dualarm65536.md)" if issue else ""),
                      "issue": issue_step,

@@ -637,7 +637,7 @@ static std::vector<size_t> farthest_order(const std::vector<std::array<double, 3
 struct FastPipe {
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  DevBuf in[2], out[2], dist[2], items[2], hq[2], pose[2];
+  DevBuf in[2], out[2], dist[2], items[2], hq[2];
   DevBuf ctl, ovf;  // per chunk counters (64 B each) and per-config overflow flags, for the whole call
   FastPipe() = default;
   FastPipe(const FastPipe&) = delete;
@@ -679,7 +679,6 @@ struct HostCst {
   DevBuf w_in, w_in2, w_out, w_out2, w_aux, w_seq, w_width;
   DevBuf f_items, f_ctl, f_overflow;  // fast-path recheck queue, counters, per-config overflow flags
   DevBuf f_hq;                        // fast-path hard cloud queries (distances mode)
-  DevBuf f_pose;                      // fast-path FP32 poses of the FK kernel
   PinBuf h_pin;                       // pinned staging of small host-memory calls
   DevBuf w_cen;                       // sphere centres of a device-memory distances call without centres
   FastPipe pipe;                      // host-memory fast calls of large batches
@@ -1826,11 +1825,9 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
   float* ddist[2];
   int4* items[2];
   void* hqb[2];
-  float* pose[2];
   const unsigned hq_cap = hard_query_cap(chunk, ns);
   for (int k = 0; k < 2; k++) {  // sized once per call, before any chunk is in flight
     hqb[k] = dist32 ? P.hq[k].ensure((size_t)hq_cap * 32) : nullptr;
-    pose[k] = (float*)P.pose[k].ensure((size_t)fast_pose_floats(C.hdr, chunk) * 4);
     din[k] = (double*)P.in[k].ensure((size_t)chunk * d * 8);
     dout[k] = (uint8_t*)P.out[k].ensure(std::max<size_t>((size_t)chunk, 16));
     ddist[k] = dist32 ? (float*)P.dist[k].ensure((size_t)chunk * ns * 4) : nullptr;
@@ -1850,7 +1847,7 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
     char* cc = ctl + i * 64;
     cuda_check(launch_fast_valid(T, C.hdr, st, din[k], n, dout[k], ddist[k], 0.1f, items[k], (unsigned int*)cc, cap, ovf + c0,
                                  (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs, hqb[k], (unsigned long long*)(cc + 48), hq_cap,
-                                 pose[k], C.tune),
+                                 C.tune),
                "is_valid_fast");
     cuda_check(cudaMemcpyAsync(out + c0, dout[k], (size_t)n, cudaMemcpyDeviceToHost, cs), "D2H copy");
     if (dist32) cuda_check(cudaMemcpyAsync(dist32 + c0 * ns, ddist[k], (size_t)(n * ns) * 4, cudaMemcpyDeviceToHost, cs), "D2H copy");
@@ -1913,9 +1910,8 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     }
     const unsigned hq_cap = hard_query_cap(B, C.n_spheres());
     void* hq = dd ? C.f_hq.ensure((size_t)hq_cap * 32) : nullptr;
-    float* pose = (float*)C.f_pose.ensure(std::max<size_t>((size_t)fast_pose_floats(C.hdr, B) * 4, 16));
     cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s, hq,
-                                 (unsigned long long*)(ctl + 48), hq_cap, pose, C.tune),
+                                 (unsigned long long*)(ctl + 48), hq_cap, C.tune),
                "is_valid_fast");
     char* pin_out = pin ? pin + up16(nq) : nullptr;
     char* pin_dist = pin ? pin_out + up16((size_t)B) : nullptr;

@@ -72,7 +72,6 @@ struct SlotF {
 // [18] eq = bound on |q - q64|_2.  A point s of the link frame then lies within et + eb |s| of
 // its FP64 position, plus the rounding of R s + t that margin32 covers.
 constexpr int kPoseF = 20;
-constexpr int kPoseUsed = 14;  // fields read after the FK: R, t, et, eb
 
 enum { ST_PASS = 0, ST_FAIL = 1, ST_MAYBE = 2 };
 constexpr int FLAG_FAIL = 1;
@@ -94,8 +93,6 @@ struct Scratch {
   HardQuery* hq;           // global hard-query queue (distances mode), or null: queries stay in the block
   unsigned long long* hq_count;  // entries reserved (64-bit: a large batch may reserve more than 2^32)
   unsigned int hq_cap;
-  const float* gpose;      // poses from k_fk32 ([slot][field][configuration], the batch's stride), or null:
-                           // each block runs the FK itself
   int st_log2;             // sphere tile: log2 of the spheres a warp row of sphere tasks holds (0: the
                            // least, 32 / configurations per block)
 };
@@ -108,6 +105,12 @@ __device__ __forceinline__ float3 xf(const float* P, float x, float y, float z) 
 // compute_approx_sin_cos (kinematics/algorithm.cpp:50-86) with the range reduction in FP64 and
 // the polynomial in FP32 (Horner form): within 8 units of roundoff (sin) and 12 (cos) of the FP64
 // value for the reduced |x| <= pi/2.
+// isfinite of a double by its exponent bits (integer instructions only)
+__device__ __forceinline__ bool finite64(double v) { return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000; }
+
+// qf = (float)q: for |q| below pi no range reduction applies, and x = q / 2 rounds to qf / 2 exactly
+// (halving commutes with rounding), so the FP64 arithmetic is skipped there with the same result.
+__device__ __forceinline__ void approx_sin_cos32_q(double q, float qf, float& s, float& c);
 __device__ __forceinline__ void approx_sin_cos32(double x, float& s, float& c) {
   const double pi = 3.14159265358979323846, half_pi = pi * 0.5;
   double cos_sign = 1.0;
@@ -126,6 +129,15 @@ __device__ __forceinline__ void approx_sin_cos32(double x, float& s, float& c) {
   c = 1.0f - xx * (0.5f - xx * (1.0f / 24.0f - xx * (1.0f / 720.0f - xx * (1.0f / 40320.0f))));
   if (cos_sign < 0.0) c = -c;
 }
+__device__ __forceinline__ void approx_sin_cos32_q(double q, float qf, float& s, float& c) {
+  if (fabsf(qf) <= 3.1415925f) {  // < pi: |q / 2| < pi / 2 in FP64 too
+    const float xf = qf * 0.5f, xx = xf * xf;
+    s = xf * (1.0f - xx * (1.0f / 6.0f - xx * (1.0f / 120.0f - xx * (1.0f / 5040.0f - xx * (1.0f / 362880.0f)))));
+    c = 1.0f - xx * (0.5f - xx * (1.0f / 24.0f - xx * (1.0f / 720.0f - xx * (1.0f / 40320.0f))));
+    return;
+  }
+  approx_sin_cos32(q * 0.5, s, c);
+}
 
 // FP32 FK of one configuration into P (n_slots x kPoseF) with error bounds against the FP64 FK
 // of the reference (update_kintree + get_link_pose; algorithm.cpp:88-210).  Bounds, u = 2^-24,
@@ -137,8 +149,8 @@ __device__ __forceinline__ void approx_sin_cos32(double x, float& s, float& c) {
 //     q -> R(q)v has derivative norm <= 6.4 |v| at |q| <= 1.001; matrix and product rounding);
 //   translation t = tp + R lt: |dt| <= |dtp| + (8 |dqp| + 24u)|lt| + 1.01 u (|tp|_1 + |lt|_1).
 // The base pose adds the rounding of q's base entries (and of their half angles).
-// Field f of slot i is P[(i * kPoseF + f) * stride]: stride 1 in a block's shared memory, the batch
-// size in the FK kernel's [slot][field][configuration] layout.
+// Field f of slot i is P[(i * kPoseF + f) * stride] (stride 1: a block's shared memory, one
+// configuration's slots in a row).
 __device__ __forceinline__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restrict__ base8, int base_type, int n_ctrl,
                                      const double* __restrict__ q, bool taylor, float* __restrict__ P, int64_t stride = 1) {
   for (int i = 0; i < nsl; i++) {
@@ -188,16 +200,17 @@ __device__ __forceinline__ void fk32(const SlotF* __restrict__ S, int nsl, const
         elt = 4.0f * kU * (s.lt1 + fabsf(th) * (fabsf(s.axis[0]) + fabsf(s.axis[1]) + fabsf(s.axis[2])));
         lid = true;
       } else {
-        const double x = q[s.qcol] * 0.5;
+        const double qd = q[s.qcol];
+        const float qf = (float)qd, xf = qf * 0.5f;  // (float)(qd / 2), exactly
         float sn, cs;
         if (taylor) {
-          approx_sin_cos32(x, sn, cs);
+          approx_sin_cos32_q(qd, qf, sn, cs);
         } else {
-          sincosf((float)x, &sn, &cs);
+          sincosf(xf, &sn, &cs);
         }
         const FQ jq{sn * s.axis[0], sn * s.axis[1], sn * s.axis[2], cs};
         lq = lid ? jq : fqmul(FQ{s.lq[0], s.lq[1], s.lq[2], s.lq[3]}, jq);
-        el = (lid ? 20.0f : 32.0f) * kU + (taylor ? 0.0f : 2.0f * kU * fabsf((float)x));
+        el = (lid ? 20.0f : 32.0f) * kU + (taylor ? 0.0f : 2.0f * kU * fabsf(xf));
         lid = false;
       }
       wq = lid ? pq : fqmul(pq, lq);
@@ -946,41 +959,14 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   const int ns = T->n_spheres, ng = T->n_groups, np = T->n_prims, npr = T->n_pairs, nsl = T->n_slots;
   const int tid = threadIdx.x;
   if (tid < CPB) sm.flags[tid] = 0;
-  // ---- 1. FK (FP32, with error bounds) -> shared memory: from k_fk32's poses when it ran (the fields
-  //         the checks read: R, t and the two bounds), else here, one thread per configuration
-  if (scr.gpose != nullptr) {
-    const int64_t stride = src.n_overflow_slots();  // the batch size
-    const int total = CPB * nsl * kPoseUsed;
-    // 8 loads in flight per thread before their stores (a load waiting on the previous store would
-    // pay the memory latency once per element)
-    for (int base = tid; base < total; base += 8 * (int)blockDim.x) {
-      float val[8];
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int idx = base + j * (int)blockDim.x;
-        const int c = idx & (CPB - 1), r = idx / CPB;  // configurations fastest: coalesced reads
-        const int f = r % kPoseUsed, i = r / kPoseUsed;
-        val[j] = idx < total && c < ncfg ? __ldg(scr.gpose + ((int64_t)i * kPoseF + f) * stride + c0 + c) : 0.f;
-      }
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int idx = base + j * (int)blockDim.x;
-        const int c = idx & (CPB - 1), r = idx / CPB;
-        const int f = r % kPoseUsed, i = r / kPoseUsed;
-        if (idx < total && c < ncfg) sm.pose[((size_t)c * nsl + i) * kPoseF + f] = val[j];
-      }
-    }
-    if (tid < ncfg && scr.gpose[(int64_t)12 * stride + c0 + tid] < 0.f) {  // k_fk32's mark of a non-finite coordinate
-      sm.flags[tid] = 2;
-      scr.overflow[src.overflow_slot(c0 + tid)] = 1;
-    }
-  } else if (tid < ncfg) {
+  // ---- 1. FK (FP32, with error bounds) -> shared memory, one thread per configuration
+  if (tid < ncfg) {
     if (src.pre_skip(c0 + tid)) {
       sm.flags[tid] = FLAG_FAIL | 2;  // already known invalid: no work
     } else {
       const double* qc = src.cfg(T, c0 + tid, qbuf + tid * T->q_dim);
       bool finite = true;
-      for (int i = 0; i < T->q_dim; i++) finite = finite && isfinite(qc[i]);
+      for (int i = 0; i < T->q_dim; i++) finite = finite && finite64(qc[i]);
       if (finite) {
         fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, sm.pose + (size_t)tid * nsl * kPoseF);
       } else {
@@ -1007,7 +993,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       float g, sd, mag;
       const PrimF& P = sm.prm[p];
       if (P.kind == PM_SDF_CLOUD) {  // the nearest-point field bounds the cloud from below
-        const float lb = grid_field32(v.C[P.cloud], gc.x, gc.y, gc.z).lb;
+        const float lb = grid_field_lb16(v.C[P.cloud], gc.x, gc.y, gc.z);
         g = lb - P.a - G.radius;
         mag = fabsf(gc.x) + fabsf(gc.y) + fabsf(gc.z) + lb;
       } else {
@@ -1061,9 +1047,12 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
       float g, sd, mag;
       if (Pr.kind == PM_SDF_CLOUD) {
         const PmGridDev& Gc = v.C[Pr.cloud];
-        const FieldLB fb = grid_field32(Gc, sc.x, sc.y, sc.z, !want_dist && check);
+        // the field's 16-bit bound first (one 2-byte load); the nearest point only where the
+        // validity-only shortcut below can use it
+        const float lb = grid_field_lb16(Gc, sc.x, sc.y, sc.z);
         const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
-        if (fb.lb - Pr.a - S.r > margin32(qmag + fb.lb) + ek + (want_dist ? cutoff : 0.f)) continue;
+        if (lb - Pr.a - S.r > margin32(qmag + lb) + ek + (want_dist ? cutoff : 0.f)) continue;
+        const FieldLB fb = !want_dist && check ? grid_field32(Gc, sc.x, sc.y, sc.z, true) : FieldLB{lb, -1, make_float4(0.f, 0.f, 0.f, 0.f)};
         if (!want_dist && check && fb.idx >= 0) {
           // the centre's nearest point is a real point: if it is certainly within reach, the
           // sphere collides and no search is needed
@@ -1425,30 +1414,6 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
   __syncthreads();
 }
 
-// FP32 FK of a batch, one thread per configuration, the poses written in [slot][field][configuration]
-// order (the batch size as the stride) so that k_fast_valid's blocks read them coalesced; the parent
-// poses read back by the FK are the thread's own writes.  A configuration with a non-finite
-// coordinate gets et = -1 in slot 0 (a bound is never negative): k_fast_valid leaves it to the exact
-// FP64 check.
-__global__ void __launch_bounds__(128) k_fk32(const PmTablesHdr* __restrict__ T, const double* __restrict__ state,
-                                              const double* __restrict__ q, int64_t B, float* __restrict__ gpose) {
-  __shared__ SlotF s_slot[PM_MAX_SLOTS];
-  __shared__ float s_base8[8];
-  TView v(T);
-  stage_slots(v, s_slot, s_base8, state);
-  __syncthreads();
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  const double* qc = q + b * T->q_dim;
-  bool finite = true;
-  for (int i = 0; i < T->q_dim; i++) finite = finite && isfinite(qc[i]);
-  if (finite) {
-    fk32(s_slot, T->n_slots, s_base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, gpose + b, B);
-  } else {
-    gpose[(int64_t)12 * B + b] = -1.0f;
-  }
-}
-
 // 64 registers a thread, stated as the occupancy target (NT threads x 65536 / (NT x 64) blocks
 // per SM): the same budget the compiler picks for NT alone, but its allocation under the explicit
 // target measured 4-8 % faster in both modes.
@@ -1509,23 +1474,18 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
   const int ns = T->n_spheres;
   const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  // each warp takes a contiguous range of the queue: queries pushed together (neighbouring spheres,
-  // the same block's configurations) then share the SM's L1
-  const int64_t per = (((n + 1) >> 1) + nw - 1) / nw * 2;  // queries per warp, even
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t k_end = min(n, (w + 1) * per);
-  int64_t k = w * per;  // the warp's pair: k (half 0), k + 1 (half 1)
+  int64_t k = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
   auto record = [&](int64_t i) {  // the half's query i
-    if (i >= k_end) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
+    if (i >= n) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
     const HardQuery h = hq[i];
     return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z, hl);
   };
   float4 rec = record(k + half);
-  while (k < k_end) {  // warp-uniform
-    const int64_t kn = k + 2;
+  while (k < n) {  // warp-uniform
+    const int64_t kn = k + 2 * nw;
     const float4 rec_n = record(kn + half);
     const int64_t i = k + half;
-    const bool have = i < k_end;  // the same on the half's lanes
+    const bool have = i < n;  // the same on the half's lanes
     HardQuery h;
     h.a = make_float4(0.f, 0.f, 0.f, 0.f);
     h.b = make_int4(0, 0, 0, 0);
@@ -1824,23 +1784,17 @@ static unsigned recheck_grid(int64_t units, int per_block, int n_sm) {
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq,
-                              unsigned long long* hq_count, unsigned int hq_cap, float* pose, const FastTuning& tune) {
+                              unsigned long long* hq_count, unsigned int hq_cap, const FastTuning& tune) {
   if (B <= 0) return cudaSuccess;
   if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   // (hard-query entries hold 32-bit configuration indices)
   const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
-              split ? hq_cap : 0u, pose, tune.sphere_tile_log2};
+              split ? hq_cap : 0u, tune.sphere_tile_log2};
   size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
   cudaError_t e;
-  if (pose) {
-    prof_begin("k_fk32", s);
-    k_fk32<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(T, state, q, B, pose);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    prof_end("k_fk32", s);
-  }
   prof_begin("k_fast_valid", s);
 #define PM_FAST_CASE(C, N)                                                                      \
   if (cpb == C && nt == N) {                                                                     \

@@ -222,7 +222,8 @@ __global__ void k_edf_final(const int16_t* __restrict__ in, int64_t n, uint8_t* 
 // `reach` and a lower bound on the centre's distance to every point (the FP32 value shrunk by the
 // rounding of d^2, of the square root and of the FP32 point coordinates).  Cells whose
 // box-to-box bound already reaches `reach` skip the search.
-__global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int2* __restrict__ out, float4* __restrict__ out_np) {
+__global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int2* __restrict__ out, float4* __restrict__ out_np,
+                        uint16_t* __restrict__ out16) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)ncx * ncy * ncz) return;
   const int cx = (int)(i % ncx), cy = (int)((i / ncx) % ncy), cz = (int)(i / ((int64_t)ncx * ncy));
@@ -238,7 +239,11 @@ __global__ void k_field(PmGridDev G, int ncx, int ncy, int ncz, float reach, int
       idx = r.idx;
     }
   }
-  out[i] = make_int2(__float_as_int(fmaxf(d * (1.0f - 1e-6f) - slack, 0.0f)), idx);
+  const float lb = fmaxf(d * (1.0f - 1e-6f) - slack, 0.0f);
+  out[i] = make_int2(__float_as_int(lb), idx);
+  // the same bound in 16 bits, rounded down to PM_FIELD16_UNIT (capped: the cap is a lower bound too)
+  const float u = floorf(lb * (1.0f / PM_FIELD16_UNIT) * (1.0f - 1e-6f));
+  out16[i] = (uint16_t)(u >= 65535.f ? 65535.f : (u > 0.f ? u : 0.f));
   float4 np = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
   if (idx >= 0) {
     np = G.p32[idx];
@@ -580,6 +585,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   uint8_t* edf = nullptr;
   float* cell_lb = nullptr;
   int2* cell_nn = nullptr;
+  uint16_t* cell_lb16 = nullptr;
   float4* cell_np = nullptr;
   float4* cell_rec = nullptr;
   int4* cand4 = nullptr;
@@ -706,6 +712,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
     {  // nearest-point field (needs the finished descriptor for its nearest-neighbour walks)
       const int64_t ncl = (int64_t)nc[0] * nc[1] * nc[2];
       if ((e = keep(ncl * 8, (void**)&cell_nn)) != cudaSuccess) break;
+      if ((e = keep(ncl * 2, (void**)&cell_lb16)) != cudaSuccess) break;
       if ((e = keep(ncl * 16, (void**)&cell_np)) != cudaSuccess) break;
       PmGridDev v = d;
       v.blk_list = nullptr;  // the walks below run without candidate lists
@@ -731,11 +738,12 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
       v.edf = edf;
       v.cell_lb = cell_lb;
       v.n_points = (int32_t)n;
-      k_field<<<nblk(ncl, 128), 128, 0, s>>>(v, nc[0], nc[1], nc[2], (float)g.field_reach, cell_nn, cell_np);
+      k_field<<<nblk(ncl, 128), 128, 0, s>>>(v, nc[0], nc[1], nc[2], (float)g.field_reach, cell_nn, cell_np, cell_lb16);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
       // per-block candidate lists
       v.cell_nn = cell_nn;
       v.cell_np = cell_np;
+      v.cell_lb16 = cell_lb16;
       int32_t *cnt = nullptr, *lstart = nullptr;
       if ((e = keep(nblocks * 4, (void**)&blk_reach)) != cudaSuccess) break;
       if ((e = keep(nblocks * 8, (void**)&blk_list)) != cudaSuccess) break;
@@ -814,6 +822,7 @@ cudaError_t grid_build(GridBuild& g, cudaStream_t s) {
   d.cell_lb = cell_lb;
   d.cell_nn = cell_nn;
   d.cell_np = cell_np;
+  d.cell_lb16 = cell_lb16;
   d.blk_list = blk_list;
   d.blk_cand = blk_cand;
   d.blk_reach = blk_reach;

@@ -17,6 +17,7 @@
 #define PM_GRID_CELLS_PER_BLOCK (PM_GRID_B * PM_GRID_B * PM_GRID_B)
 #define PM_CL_UNITS 16  // distance quantum of the cell lists: the fine cell edge / 16
 #define PM_GRID_SB 4    // blocks per super-block edge (the coarse level of the unbounded searches)
+#define PM_FIELD16_UNIT 2.5e-4f  // metres per unit of the 16-bit field bounds
 
 enum { PM_FK_STATE = 0, PM_FK_REV = 1, PM_FK_PRIS = 2 };
 enum { PM_BASE_FIXED = 0, PM_BASE_FLOATING = 1, PM_BASE_PLANAR = 2 };
@@ -89,6 +90,8 @@ struct PmGridDev {
                            // within field_reach)
   const float4* cell_np;   // per fine cell: that nearest point itself (x y z as p32, w = its index as int
                            // bits, -1: none), so a query reads point and index in one load
+  const uint16_t* cell_lb16;  // per fine cell: cell_nn's bound in units of PM_FIELD16_UNIT, rounded down (capped
+                           // at 65535): a 2-byte copy for the checks that need only the bound
   float field_reach;       // cell_nn searched up to this distance from each centre
   int32_t pad_nn;
   const int2* blk_list;    // per block: [first, end) of its candidate list in blk_cand (first = -1: none)

@@ -317,6 +317,35 @@ __device__ __forceinline__ FieldLB grid_field32(const PmGridDev& G, float qx, fl
   return f;
 }
 
+// grid_field32's lower bound from the 16-bit copy of the field (at most PM_FIELD16_UNIT looser): one
+// 2-byte load, for the checks that need no nearest point.
+__device__ __forceinline__ float grid_field_lb16(const PmGridDev& G, float qx, float qy, float qz) {
+  if (G.n_points <= 0) return INFINITY;
+  const float cellf = G.cell32;
+  const float qa[3] = {qx, qy, qz};
+  const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
+  int cc[3];
+  bool inside = true;
+  for (int a = 0; a < 3; a++) {
+    const float t = floorf((qa[a] - G.o32[a]) * G.inv_cell32);
+    if (!(t >= 0.f && t <= (float)(nc[a] - 1))) inside = false;
+    cc[a] = inside ? (int)t : 0;
+  }
+  if (!inside) {  // as grid_field32: the distance to the box of the points
+    float d2 = 0.f;
+    for (int a = 0; a < 3; a++) {
+      const float gap = fmaxf(fmaxf(G.box_lo32[a] - qa[a], qa[a] - G.box_hi32[a]), 0.f);
+      d2 = fmaf(gap, gap, d2);
+    }
+    return fmaxf(sqrtf(d2) * (1.0f - 1e-6f) - 4e-6f, 0.f);
+  }
+  const unsigned short u = __ldg(G.cell_lb16 + (cc[0] + nc[0] * (cc[1] + (int64_t)nc[1] * cc[2])));
+  const float dx = qx - field_centre(G.o32[0], cc[0], cellf), dy = qy - field_centre(G.o32[1], cc[1], cellf),
+              dz = qz - field_centre(G.o32[2], cc[2], cellf);
+  const float off = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * (1.0f + 1e-6f) + 1e-7f;
+  return fmaxf((float)u * PM_FIELD16_UNIT * (1.0f - 1e-6f) - off, 0.f);
+}
+
 // FP32 squared distance from q to point idx, the expression of every nearest-neighbour walk.
 __device__ __forceinline__ float point_d2_32(const PmGridDev& G, int idx, float qx, float qy, float qz) {
   const float4 p = __ldg(G.p32 + idx);

@@ -53,14 +53,10 @@ struct FastTuning {
 };
 // hq (hq_cap 32-byte entries) and hq_count (zeroed by the caller): with distances, the hard cloud
 // queries are answered by a second kernel over this global queue; null keeps them in the block.
-// pose (fast_pose_floats(h, B) floats): the FP32 FK runs first as its own kernel into it; null: each
-// block runs the FK of its configurations.
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq = nullptr,
-                              unsigned long long* hq_count = nullptr, unsigned int hq_cap = 0, float* pose = nullptr,
-                              const FastTuning& tune = FastTuning());
-inline int64_t fast_pose_floats(const PmTablesHdr& h, int64_t B) { return (int64_t)h.n_slots * 20 * B; }
+                              unsigned long long* hq_count = nullptr, unsigned int hq_cap = 0, const FastTuning& tune = FastTuning());
 
 cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
                               int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,
