@@ -829,8 +829,13 @@ def main():
     for _ in range(args.warmup):
         step()
     barrier()
-    _lib.profile_read("*")
-    _lib.profile_enable(True)
+    # The step as a CUDA graph of the same API call (captured after the warm-up): the replay launches
+    # its memsets and kernels without the per-call host work in between.  The eager call is timed
+    # below as well.
+    graph = _capture(step)
+    for _ in range(args.warmup):
+        graph.replay()
+    barrier()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     total_ms = 0.0
@@ -839,10 +844,27 @@ def main():
             flush.fill_(1.0)
             barrier()
             start.record(stream)
-            step()
+            graph.replay()
             end.record(stream)
             end.synchronize()
             total_ms += start.elapsed_time(end)
+    barrier()
+    total_ms = replicas.max_over_ranks(total_ms, dist, dev)
+    ms_per_step = total_ms / args.steps
+    value = world * B * args.steps / (total_ms / 1e3)
+    # the same steps eagerly (one API call each), with the library's per-kernel event timing: the
+    # kernel durations of the roofline and the launch count
+    _lib.profile_read("*")
+    _lib.profile_enable(True)
+    eager_ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        barrier()
+        start.record(stream)
+        step()
+        end.record(stream)
+        end.synchronize()
+        eager_ms += start.elapsed_time(end)
     barrier()
     _lib.profile_enable(False)
     k_ms, k_n = _lib.profile_read("k_fast_valid")
@@ -850,9 +872,7 @@ def main():
     r_ms, r_n = _lib.profile_read("k_fast_recheck")
     rest_ms, rest_n = _lib.profile_read("*")
     all_n = k_n + h_n + r_n + rest_n
-    total_ms = replicas.max_over_ranks(total_ms, dist, dev)
-    ms_per_step = total_ms / args.steps
-    value = world * B * args.steps / (total_ms / 1e3)
+    eager_ms = replicas.max_over_ranks(eager_ms, dist, dev) / args.steps
 
     # validity-only fast path and the plain FP64 method on the same batch
     def timed(fn, n):
@@ -970,6 +990,10 @@ def main():
                                    "sphere_tile_0": "the least tile, 32 / configs_per_block spheres per warp row"},
                                "cloud_grid": sdf.stats()}),
         "e2e": {"value": e2e_value, "unit": "configs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "step": "one CUDA-graph replay of is_valid_fast(Q, distances=True) on the resident batch (memsets, k_fast_valid, "
+                "k_hard_queries, k_fast_recheck); kernel durations from the same steps run eagerly right after",
+        "api_eager": {"value": world * B / (eager_ms / 1e3), "unit": "configs/s", "ms_per_step": eager_ms,
+                      "what": "the same step as one eager API call (host work between the launches included)"},
         "gpu_launches": all_n,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": hbm_kind,

@@ -727,6 +727,40 @@ struct HostCst {
     return d_tables.as<PmTablesHdr>();
   }
 
+  // The fast kernels' two-thread FK: the trunk (the slots up to the first one with two children,
+  // and every slot outside the subtrees below it) in phase 0 by thread 0; then the subtrees of the
+  // branching slot's children in phase 1, spread over the two threads by size (largest first onto
+  // the lighter thread).  A slot's parent is then computed earlier by the same thread or in phase 0.
+  // Without a branching slot everything is phase 0, thread 0.
+  static void split_slots(std::vector<PmSlot>& slots) {
+    const int n = (int)slots.size();
+    std::vector<std::vector<int>> kids(n);
+    for (int i = 0; i < n; i++)
+      if (slots[i].parent >= 0) kids[slots[i].parent].push_back(i);
+    int br = -1;
+    for (int i = 0; i < n && br < 0; i++)
+      if (kids[i].size() >= 2) br = i;
+    for (auto& s : slots) s.split = 0;
+    if (br < 0) return;
+    std::vector<int> size(n, 1);
+    for (int i = n - 1; i >= 0; i--)  // parents come first: children's sizes are final here
+      if (slots[i].parent >= 0) size[slots[i].parent] += size[i];
+    std::vector<int> order = kids[br];
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return size[a] > size[b]; });
+    int load[2] = {0, 0};
+    std::vector<int> owner(n, -1);
+    for (int c : order) {
+      const int t = load[1] < load[0] ? 1 : 0;
+      load[t] += size[c];
+      owner[c] = t;
+    }
+    for (int i = 0; i < n; i++) {  // a slot inherits its subtree root's thread
+      const int p = slots[i].parent;
+      if (owner[i] < 0 && p >= 0 && owner[p] >= 0) owner[i] = owner[p];
+      slots[i].split = owner[i] < 0 ? 0 : (2 | owner[i]);
+    }
+  }
+
   void build_tables() {
     HostModel& m = *kin;
     const int nl = m.n_link();
@@ -778,6 +812,7 @@ struct HostCst {
         if (in_subtree(l, m.joints[ids[c]].child)) rel |= (1ull << c);
       s.relevant = rel;
     }
+    split_slots(slots);
     std::vector<PmJoint> jrec(ids.size());
     for (size_t c = 0; c < ids.size(); c++) {
       const HostJoint& j = m.joints[ids[c]];

@@ -62,6 +62,7 @@ struct GroupF {
 // slot without a control joint, taken from the model state when the block starts).
 struct SlotF {
   int parent, mode, qcol, lid;
+  int split;  // PmSlot::split: the FK phase and thread that compute this slot
   float axis[3];
   float lq[4];
   float lt[3];
@@ -151,10 +152,13 @@ __device__ __forceinline__ void approx_sin_cos32_q(double q, float qf, float& s,
 // The base pose adds the rounding of q's base entries (and of their half angles).
 // Field f of slot i is P[(i * kPoseF + f) * stride] (stride 1: a block's shared memory, one
 // configuration's slots in a row).
+// want >= 0: only the slots whose split equals it (one phase of one thread of the two-thread FK).
 __device__ __forceinline__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restrict__ base8, int base_type, int n_ctrl,
-                                     const double* __restrict__ q, bool taylor, float* __restrict__ P, int64_t stride = 1) {
+                                     const double* __restrict__ q, bool taylor, float* __restrict__ P, int64_t stride = 1,
+                                     int want = -1) {
   for (int i = 0; i < nsl; i++) {
     const SlotF s = S[i];
+    if (want >= 0 && s.split != want) continue;
     float* o = P + (int64_t)i * kPoseF * stride;
     FQ wq;
     float wt[3], eq, et;
@@ -958,24 +962,43 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   const PmTablesHdr* T = v.T;
   const int ns = T->n_spheres, ng = T->n_groups, np = T->n_prims, npr = T->n_pairs, nsl = T->n_slots;
   const int tid = threadIdx.x;
-  if (tid < CPB) sm.flags[tid] = 0;
-  // ---- 1. FK (FP32, with error bounds) -> shared memory, one thread per configuration
-  if (tid < ncfg) {
-    if (src.pre_skip(c0 + tid)) {
-      sm.flags[tid] = FLAG_FAIL | 2;  // already known invalid: no work
-    } else {
-      const double* qc = src.cfg(T, c0 + tid, qbuf + tid * T->q_dim);
-      bool finite = true;
-      for (int i = 0; i < T->q_dim; i++) finite = finite && finite64(qc[i]);
-      if (finite) {
-        fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qc, T->base_type == PM_BASE_FIXED, sm.pose + (size_t)tid * nsl * kPoseF);
-      } else {
-        // a NaN or infinite coordinate makes every FP32 bound NaN, and no decision would be taken:
-        // the exact FP64 check of the recheck kernel decides, as for an overflowing queue
-        sm.flags[tid] = 2;
-        scr.overflow[src.overflow_slot(c0 + tid)] = 1;
+  // ---- 1. FK (FP32, with error bounds) -> shared memory, two threads per configuration (threads 2c
+  //         and 2c + 1): the trunk of the slot tree by the first, then one subtree set each (the
+  //         host's split); the configuration goes to qbuf so that both threads read it
+  {
+    const int fc = tid >> 1, fth = tid & 1;
+    const int qd = T->q_dim;
+    const bool taylor = T->base_type == PM_BASE_FIXED;
+    float* P = sm.pose + (size_t)fc * nsl * kPoseF;
+    if (fth == 0 && fc < CPB) {
+      int fl = 0;
+      if (fc < ncfg) {
+        if (src.pre_skip(c0 + fc)) {
+          fl = FLAG_FAIL | 2;  // already known invalid: no work
+        } else {
+          double* qb = qbuf + fc * qd;
+          const double* qc = src.cfg(T, c0 + fc, qb);
+          bool finite = true;
+          for (int i = 0; i < qd; i++) {
+            const double x = qc[i];
+            finite = finite && finite64(x);
+            qb[i] = x;
+          }
+          if (finite) {
+            fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qb, taylor, P, 1, 0);
+          } else {
+            // a NaN or infinite coordinate makes every FP32 bound NaN, and no decision would be taken:
+            // the exact FP64 check of the recheck kernel decides, as for an overflowing queue
+            fl = 2;
+            scr.overflow[src.overflow_slot(c0 + fc)] = 1;
+          }
+        }
       }
+      sm.flags[fc] = fl;
     }
+    __syncthreads();
+    if (fc < ncfg && !(sm.flags[fc] & 2))
+      fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qbuf + fc * qd, taylor, P, 1, 2 | fth);
   }
   __syncthreads();
   const bool want_dist = dist32 != nullptr;
@@ -1337,6 +1360,7 @@ __device__ void stage_slots(const TView& v, SlotF* __restrict__ slot, float* __r
     f.parent = S.parent;
     f.mode = S.mode;
     f.qcol = S.qcol;
+    f.split = S.split;
     for (int k = 0; k < 3; k++) f.axis[k] = (float)S.axis[k];
     double lt[3];
     if (S.mode == PM_FK_STATE) {

@@ -35,7 +35,8 @@ struct PmSlot {
   int32_t mode;             // PM_FK_STATE | PM_FK_REV | PM_FK_PRIS
   int32_t qcol;             // q column of the control joint (REV/PRIS)
   int32_t origin_identity;  // joint origin orientation flag |w-1| < 1e-6 (kinematics.cpp:110-113)
-  int32_t pad;
+  int32_t split;            // two-thread FP32 FK: phase << 1 | thread (phase 0: the trunk; phase 1: each
+                            // thread its own subtrees under the trunk's branching slot)
   uint64_t relevant;        // bit i: control joint i moves this link (rptable, kinematics.cpp:340-363)
   double axis[3];
   double oq[4];             // joint origin quaternion x y z w
