@@ -152,13 +152,15 @@ __device__ __forceinline__ void approx_sin_cos32_q(double q, float qf, float& s,
 // The base pose adds the rounding of q's base entries (and of their half angles).
 // Field f of slot i is P[(i * kPoseF + f) * stride] (stride 1: a block's shared memory, one
 // configuration's slots in a row).
-// want >= 0: only the slots whose split equals it (one phase of one thread of the two-thread FK).
+// list: the slots to compute, in order (one phase of one thread of the two-thread FK), or null: all
+// nsl.  The two threads of a configuration walk their own lists in step, so a warp computes both
+// threads' k-th slots with one instruction stream.
 __device__ __forceinline__ void fk32(const SlotF* __restrict__ S, int nsl, const float* __restrict__ base8, int base_type, int n_ctrl,
                                      const double* __restrict__ q, bool taylor, float* __restrict__ P, int64_t stride = 1,
-                                     int want = -1) {
-  for (int i = 0; i < nsl; i++) {
+                                     const unsigned char* list = nullptr) {
+  for (int k = 0; k < nsl; k++) {
+    const int i = list ? list[k] : k;
     const SlotF s = S[i];
-    if (want >= 0 && s.split != want) continue;
     float* o = P + (int64_t)i * kPoseF * stride;
     FQ wq;
     float wt[3], eq, et;
@@ -870,6 +872,9 @@ __device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int6
 struct Smem {
   double* qbuf;  // generated configurations (edges)
   int2* hq;      // hard cloud queries: (cfg << 16 | sphere, primitive)
+  unsigned char* fkl;  // the two-thread FK's slot lists: [0, 64) phase 0, [64, 128) and [128, 192) the
+                       // two threads of phase 1; fkn[0..2] their lengths
+  int* fkn;
   int* hq_n;     // [0] pushed, [1] popped
   int* sdist;    // per (cfg, sphere): running minimum signed distance, order-preserving int
   float* pose;   // [cfg][slot][kPoseF]
@@ -985,7 +990,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
             qb[i] = x;
           }
           if (finite) {
-            fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qb, taylor, P, 1, 0);
+            fk32(sm.slot, sm.fkn[0], sm.base8, T->base_type, T->n_ctrl, qb, taylor, P, 1, sm.fkl);
           } else {
             // a NaN or infinite coordinate makes every FP32 bound NaN, and no decision would be taken:
             // the exact FP64 check of the recheck kernel decides, as for an overflowing queue
@@ -998,7 +1003,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     }
     __syncthreads();
     if (fc < ncfg && !(sm.flags[fc] & 2))
-      fk32(sm.slot, nsl, sm.base8, T->base_type, T->n_ctrl, qbuf + fc * qd, taylor, P, 1, 2 | fth);
+      fk32(sm.slot, sm.fkn[1 + fth], sm.base8, T->base_type, T->n_ctrl, qbuf + fc * qd, taylor, P, 1, sm.fkl + (1 + fth) * PM_MAX_SLOTS);
   }
   __syncthreads();
   const bool want_dist = dist32 != nullptr;
@@ -1294,7 +1299,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
 
 // Shared-memory layout of a fast block; every array starts on a 16-byte boundary.
 struct SmemLayout {
-  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, hq_n, hq, sdist, total;
+  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, fkl, hq_n, hq, sdist, total;
 };
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb, bool want_dist) {
@@ -1320,6 +1325,8 @@ __host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb,
   o = a16(o + sizeof(unsigned) * (size_t)cpb * h.n_groups);
   L.qbuf = o;
   o = a16(o + sizeof(double) * (size_t)cpb * h.q_dim);
+  L.fkl = o;
+  o = a16(o + 3 * PM_MAX_SLOTS + 3 * sizeof(int));
   L.hq_n = o;
   o = a16(o + 16);
   L.hq = o;
@@ -1343,6 +1350,8 @@ __device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
   sm.flags = reinterpret_cast<int*>(p + L.flags);
   sm.cull = reinterpret_cast<unsigned*>(p + L.cull);
   sm.qbuf = reinterpret_cast<double*>(p + L.qbuf);
+  sm.fkl = p + L.fkl;
+  sm.fkn = reinterpret_cast<int*>(p + L.fkl + 3 * PM_MAX_SLOTS);
   sm.hq_n = reinterpret_cast<int*>(p + L.hq_n);
   sm.hq = reinterpret_cast<int2*>(p + L.hq);        // only with a point cloud
   sm.sdist = reinterpret_cast<int*>(p + L.sdist);   // only with distance output (the last array)
@@ -1435,6 +1444,14 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
     sm.prm[i] = f;
   }
   for (int i = tid; i < T->n_pairs; i += blockDim.x) sm.pairs[i] = make_int2(v.pairs[2 * i], v.pairs[2 * i + 1]);
+  if (tid == 0) {  // the two-thread FK's slot lists, parents first (the slot order)
+    int n[3] = {0, 0, 0};
+    for (int i = 0; i < T->n_slots; i++) {
+      const int sp = v.S[i].split, l = sp == 0 ? 0 : (sp == 2 ? 1 : 2);
+      sm.fkl[l * PM_MAX_SLOTS + n[l]++] = (unsigned char)i;
+    }
+    for (int l = 0; l < 3; l++) sm.fkn[l] = n[l];
+  }
   __syncthreads();
 }
 

@@ -1,8 +1,10 @@
 """Small, self-contained launches for profiling: the fast collision check of 65,536 dual-arm
 configurations against the 200k-point box-surface cloud, validity only (``valid``) or with the
 per-sphere distances (``dist``), three launches each; one fused IK descent (8192 problems x 50
-steps, ``ik``); one trajectory cost + gradient (512 trajectories, ``traj``).
-python profile_cases.py [valid|dist|ik|traj|all]"""
+steps, ``ik``); one trajectory cost + gradient (512 trajectories, ``traj``); three fast edge
+pipelines over 1024 chain edges (``edges``); two plain FP64 batches of 8192 dual-arm configurations
+(``plain``).
+python profile_cases.py [valid|dist|ik|traj|edges|plain|all]"""
 import sys
 from pathlib import Path
 
@@ -22,6 +24,36 @@ def fast(distances: bool, n: int = 65536, launches: int = 3):
     Q = torch.tensor(W.dualarm_configs(n), device="cuda")
     for _ in range(launches):
         cst.is_valid_fast(Q, distances=distances)
+    torch.cuda.synchronize()
+
+
+def edges(launches: int = 3):
+    """C1: 1024 edges (1-120 waypoints) on the 7-joint chain, the fast edge pipeline."""
+    import torch
+
+    from plainmp_gb300 import BoxMotionValidator, scenes
+    from plainmp_gb300 import workloads as W
+
+    _, cst, _ = scenes.make_constraint(W.chain7_robot(), W.chain7_scene())
+    s1, s2 = W.chain7_edges(1024)
+    S1, S2 = torch.tensor(s1, device="cuda"), torch.tensor(s2, device="cuda")
+    mv = BoxMotionValidator(cst, [0.05] * 7)
+    for _ in range(launches):
+        mv.check_motion_fast(S1, S2)
+    torch.cuda.synchronize()
+
+
+def plain(n: int = 8192, launches: int = 2):
+    """The plain FP64 method (k_is_valid64) on n dual-arm configurations against the 200k-point cloud."""
+    import torch
+
+    from plainmp_gb300 import scenes
+    from plainmp_gb300 import workloads as W
+
+    _, cst, _ = scenes.make_constraint(W.dualarm_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0))
+    Q = torch.tensor(W.dualarm_configs(n), device="cuda")
+    for _ in range(launches):
+        cst.is_valid_batch(Q)
     torch.cuda.synchronize()
 
 
@@ -67,3 +99,7 @@ if __name__ == "__main__":
         ik()
     if which in ("traj", "all"):
         traj()
+    if which in ("edges", "all"):
+        edges()
+    if which in ("plain", "all"):
+        plain()
