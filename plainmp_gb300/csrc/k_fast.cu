@@ -869,10 +869,6 @@ __device__ __forceinline__ void push_item(const Scratch& s, const Src& src, int6
   }
 }
 
-// Room of a block's hard-query queue: half of its (configuration, sphere) tasks (the dual-arm cloud
-// batch queues about 6 %); a block whose queries do not fit answers the rest in the sphere task.
-__host__ __device__ inline int hq_capacity(const PmTablesHdr& h, int cpb) { return h.n_clouds > 0 ? (cpb * h.n_spheres + 1) / 2 : 0; }
-
 struct Smem {
   double* qbuf;  // generated configurations (edges)
   int2* hq;      // hard cloud queries: (cfg << 16 | sphere, primitive)
@@ -881,7 +877,6 @@ struct Smem {
   int* fkn;
   int* hq_n;     // [0] pushed, [1] popped
   int* sdist;    // per (cfg, sphere): running minimum signed distance, order-preserving int
-  float* fld;    // per (cfg, sphere): the first cloud's field bound at the sphere centre (+inf: none)
   float* pose;   // [cfg][slot][kPoseF]
   SlotF* slot;
   float* base8;  // fixed base pose: q xyzw, t xyz
@@ -1036,41 +1031,6 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     }
     sm.cull[c * ng + gi] = mask;
   }
-  // ---- 2b. the first cloud's field bound at the sphere centres, into shared memory: 16-bit records
-  //          (L2-resident), loads four in flight per thread, so a block pays the latency once, not once
-  //          per sphere task
-  const int pc = sm.hq_n[3];  // the first cloud primitive (-1: none), from the staging
-  constexpr int cpb_l = CPB == 16 ? 4 : (CPB == 32 ? 5 : (CPB == 64 ? 6 : 7));
-  if (pc >= 0) {  // block-uniform
-    const PmGridDev& Gc = v.C[sm.prm[pc].cloud];
-    const int total = CPB * ns;
-    for (int base = tid; base < total; base += 4 * (int)blockDim.x) {
-      int raw[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int idx = base + j * (int)blockDim.x;
-        const int c = idx & (CPB - 1), si = idx >> cpb_l;
-        raw[j] = -1;
-        if (idx < total && c < ncfg && !(sm.flags[c] & 2)) {
-          const SphereF S = sm.sph[si];
-          const float* P = sm.pose + ((size_t)c * nsl + sm.grp[S.group].slot) * kPoseF;
-          const float3 sc = xf(P, S.x, S.y, S.z);
-          raw[j] = grid_field16_raw(Gc, sc.x, sc.y, sc.z);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int idx = base + j * (int)blockDim.x;
-        const int c = idx & (CPB - 1), si = idx >> cpb_l;
-        if (idx < total && c < ncfg && !(sm.flags[c] & 2)) {
-          const SphereF S = sm.sph[si];
-          const float* P = sm.pose + ((size_t)c * nsl + sm.grp[S.group].slot) * kPoseF;
-          const float3 sc = xf(P, S.x, S.y, S.z);  // as above
-          sm.fld[c * ns + si] = grid_field16_lb(Gc, sc.x, sc.y, sc.z, raw[j]);
-        }
-      }
-    }
-  }
   __syncthreads();
   // ---- 3a. sphere tasks (primitives in-thread; cloud queries near the cloud are queued) and
   //          self-pair tasks
@@ -1079,12 +1039,13 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
     sm.hq_n[1] = 0;
   }
   __syncthreads();
-  const int hq_cap = hq_capacity(*T, CPB);
+  const int hq_cap = T->n_clouds > 0 ? CPB * ns : 0;
   // Sphere tasks in warp rows of 32 / ST configurations (fastest) x ST spheres; ST = 2^stl is the
   // sphere tile (autotuned), at least 32 / CPB so that a row holds every configuration once.  A small
   // tile puts the same sphere on neighbouring lanes (shared records); a large one keeps a
   // configuration's neighbouring spheres, and so their field cells, on one warp.  Pair tasks
   // follow, numbered with the configuration fastest.  CPB is a power of two: no division.
+  constexpr int cpb_l = CPB == 16 ? 4 : (CPB == 32 ? 5 : (CPB == 64 ? 6 : 7));
   const int stl = max(min(scr.st_log2, 5), cpb_l >= 5 ? 0 : 5 - cpb_l);
   const int rl = 5 - stl, ncb_l = cpb_l - rl;  // configurations per row, rows per sphere tile (log2)
   const int n_sph_tasks = (((ns + (1 << stl) - 1) >> stl) << ncb_l) << 5;
@@ -1116,7 +1077,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
         const PmGridDev& Gc = v.C[Pr.cloud];
         // the field's 16-bit bound first (one 2-byte load); the nearest point only where the
         // validity-only shortcut below can use it
-        const float lb = p == pc ? sm.fld[c * ns + si] : grid_field_lb16(Gc, sc.x, sc.y, sc.z);
+        const float lb = grid_field_lb16(Gc, sc.x, sc.y, sc.z);
         const float qmag = fabsf(sc.x) + fabsf(sc.y) + fabsf(sc.z);
         if (lb - Pr.a - S.r > margin32(qmag + lb) + ek + (want_dist ? cutoff : 0.f)) continue;
         const FieldLB fb = !want_dist && check ? grid_field32(Gc, sc.x, sc.y, sc.z, true) : FieldLB{lb, -1, make_float4(0.f, 0.f, 0.f, 0.f)};
@@ -1338,7 +1299,7 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
 
 // Shared-memory layout of a fast block; every array starts on a 16-byte boundary.
 struct SmemLayout {
-  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, fkl, hq_n, hq, fld, sdist, total;
+  size_t pose, slot, base8, sph, grp, prm, pairs, flags, cull, qbuf, fkl, hq_n, hq, sdist, total;
 };
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb, bool want_dist) {
@@ -1369,9 +1330,7 @@ __host__ __device__ inline SmemLayout smem_layout(const PmTablesHdr& h, int cpb,
   L.hq_n = o;
   o = a16(o + 16);
   L.hq = o;
-  o = a16(o + sizeof(int2) * (size_t)hq_capacity(h, cpb));
-  L.fld = o;
-  o = a16(o + (h.n_clouds > 0 ? sizeof(float) * (size_t)cpb * h.n_spheres : 0));
+  o = a16(o + (h.n_clouds > 0 ? sizeof(int2) * (size_t)cpb * h.n_spheres : 0));
   L.sdist = o;
   o = a16(o + (want_dist ? sizeof(int) * (size_t)cpb * h.n_spheres : 0));
   L.total = o;
@@ -1395,7 +1354,6 @@ __device__ Smem carve(unsigned char* p, const PmTablesHdr* T, int cpb) {
   sm.fkn = reinterpret_cast<int*>(p + L.fkl + 3 * PM_MAX_SLOTS);
   sm.hq_n = reinterpret_cast<int*>(p + L.hq_n);
   sm.hq = reinterpret_cast<int2*>(p + L.hq);        // only with a point cloud
-  sm.fld = reinterpret_cast<float*>(p + L.fld);     // only with a point cloud
   sm.sdist = reinterpret_cast<int*>(p + L.sdist);   // only with distance output (the last array)
   return sm;
 }
@@ -1486,12 +1444,6 @@ __device__ void stage_tables(const TView& v, const Smem& sm, const double* __res
     sm.prm[i] = f;
   }
   for (int i = tid; i < T->n_pairs; i += blockDim.x) sm.pairs[i] = make_int2(v.pairs[2 * i], v.pairs[2 * i + 1]);
-  if (tid == 32) {  // the first cloud primitive (-1: none)
-    int pc = -1;
-    for (int i = 0; i < T->n_prims && pc < 0; i++)
-      if (v.P[i].kind == PM_SDF_CLOUD) pc = i;
-    sm.hq_n[3] = pc;
-  }
   if (tid == 0) {  // the two-thread FK's slot lists, parents first (the slot order)
     int n[3] = {0, 0, 0};
     for (int i = 0; i < T->n_slots; i++) {

@@ -346,41 +346,6 @@ __device__ __forceinline__ float grid_field_lb16(const PmGridDev& G, float qx, f
   return fmaxf((float)u * PM_FIELD16_UNIT * (1.0f - 1e-6f) - off, 0.f);
 }
 
-// grid_field_lb16 in two steps, so that loads can be issued in batches: the 16-bit record of q's
-// fine cell (-1: q outside the grid), then the bound from it (the same value grid_field_lb16 gives).
-__device__ __forceinline__ int grid_field16_raw(const PmGridDev& G, float qx, float qy, float qz) {
-  if (G.n_points <= 0) return -1;
-  const float qa[3] = {qx, qy, qz};
-  const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
-  int cc[3];
-  for (int a = 0; a < 3; a++) {
-    const float t = floorf((qa[a] - G.o32[a]) * G.inv_cell32);
-    if (!(t >= 0.f && t <= (float)(nc[a] - 1))) return -1;
-    cc[a] = (int)t;
-  }
-  return (int)__ldg(G.cell_lb16 + (cc[0] + nc[0] * (cc[1] + (int64_t)nc[1] * cc[2])));
-}
-__device__ __forceinline__ float grid_field16_lb(const PmGridDev& G, float qx, float qy, float qz, int raw) {
-  if (G.n_points <= 0) return INFINITY;
-  const float qa[3] = {qx, qy, qz};
-  if (raw < 0) {  // outside the grid: the distance to the box of the points, as grid_field32
-    float d2 = 0.f;
-    for (int a = 0; a < 3; a++) {
-      const float gap = fmaxf(fmaxf(G.box_lo32[a] - qa[a], qa[a] - G.box_hi32[a]), 0.f);
-      d2 = fmaf(gap, gap, d2);
-    }
-    return fmaxf(sqrtf(d2) * (1.0f - 1e-6f) - 4e-6f, 0.f);
-  }
-  const float cellf = G.cell32;
-  float d[3];
-  for (int a = 0; a < 3; a++) {
-    const float t = floorf((qa[a] - G.o32[a]) * G.inv_cell32);
-    d[a] = qa[a] - field_centre(G.o32[a], (int)t, cellf);
-  }
-  const float off = sqrtf(fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]))) * (1.0f + 1e-6f) + 1e-7f;
-  return fmaxf((float)raw * PM_FIELD16_UNIT * (1.0f - 1e-6f) - off, 0.f);
-}
-
 // FP32 squared distance from q to point idx, the expression of every nearest-neighbour walk.
 __device__ __forceinline__ float point_d2_32(const PmGridDev& G, int idx, float qx, float qy, float qz) {
   const float4 p = __ldg(G.p32 + idx);
