@@ -20,7 +20,8 @@ def fast(distances: bool, n: int = 65536, launches: int = 3):
     from plainmp_gb300 import workloads as W
 
     _, cst, _ = scenes.make_constraint(W.dualarm_robot(), W.Scene(cloud=W.box_surface_cloud(), cloud_radius=0.0))
-    cst.set_fast_launch(16, 256)  # the shape the benchmark's autotuner picks for this workload
+    cst.set_fast_launch(16, 256)  # the shape and sphere tile the benchmark's autotuner picks for this workload
+    cst.set_fast_tuning(8, 4, 32, 128)
     Q = torch.tensor(W.dualarm_configs(n), device="cuda")
     for _ in range(launches):
         cst.is_valid_fast(Q, distances=distances)

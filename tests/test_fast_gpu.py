@@ -416,3 +416,19 @@ def test_fast_queries_beyond_the_cell_lists(oracle):
     assert np.array_equal(ok, ref)
     d64 = np.minimum(cst.sphere_distances(Q[::4]), CUTOFF)
     assert np.abs(d32[::4].astype(np.float64) - d64).max() < DIST_TOL
+
+
+def test_fast_refuses_tables_beyond_the_queue_records():
+    """The fast path's queue records hold 15 bits of primitive index: a scene of 32,768 primitives
+    is refused with a clear error (the plain method still checks it), where 32,767 would only run
+    out of shared memory."""
+    from plainmp_gb300 import Pose, SphereSDF, UnionSDF
+
+    robot = W.chain7_robot()
+    _, cst, _ = scenes.make_constraint(robot, None, self_collision=False)
+    far = [SphereSDF(0.01, Pose(np.array([10.0 + 0.001 * i, 0.0, 0.0]), np.eye(3))) for i in range(32768)]
+    cst.set_sdf(UnionSDF(far))
+    Q = W.chain7_configs(4, seed=47)
+    assert cst.is_valid_batch(Q).all()
+    with pytest.raises(ValueError, match="32767 primitives"):
+        cst.is_valid_fast(Q)
