@@ -56,7 +56,8 @@ struct Layout {
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline Layout make_layout(int n_slots, int n_sph, int n_prims, int qd) {
+// groups: units in flight per block (kNW warps times the units per warp)
+__host__ __device__ inline Layout make_layout(int n_slots, int n_sph, int n_prims, int qd, int groups = kNW) {
   Layout L;
   L.n_slots = n_slots;
   L.n_sph = n_sph;
@@ -76,7 +77,7 @@ __host__ __device__ inline Layout make_layout(int n_slots, int n_sph, int n_prim
   // per warp: q, grad, target/pose wrench scratch (16), slot work, sphere adjoints (6 each)
   L.warp_floats = (size_t)2 * L.qpad + 16 + (size_t)kSlotF * n_slots + (size_t)6 * n_sph;
   L.warp_floats = (L.warp_floats + 3) & ~(size_t)3;
-  L.total = o + sizeof(float) * L.warp_floats * kNW;
+  L.total = o + sizeof(float) * L.warp_floats * groups;
   return L;
 }
 
@@ -193,8 +194,11 @@ __device__ __forceinline__ WS warp_ws(const Layout& L, char* smem, int w) {
   return s;
 }
 
+// Sum over a unit's GW lanes (a whole warp, or each aligned GW-lane part of it: the xor offsets
+// stay inside).
+template <int GW = 32>
 __device__ __forceinline__ float warp_sum(float v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = GW / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
@@ -204,9 +208,11 @@ __device__ __forceinline__ void cross3(const float a[3], const float b[3], float
   o[2] = fmaf(a[0], b[1], -a[1] * b[0]);
 }
 
-// FK of the warp's configuration ws.q into ws.sw.
+// FK of the unit's configuration ws.q into ws.sw (GW lanes per unit; the units of a warp run it
+// in step).
+template <int GW = 32>
 __device__ void warp_fk(const Tab& t, const WS& ws, int lane) {
-  for (int i = lane; i < t.n_slots; i += 32) {
+  for (int i = lane; i < t.n_slots; i += GW) {
     const GSlot& s = t.slot[i];
     float* w = ws.sw + (size_t)i * kSlotF;
     if (s.parent < 0) continue;
@@ -282,7 +288,7 @@ __device__ void warp_fk(const Tab& t, const WS& ws, int lane) {
     }
   }
   __syncwarp();
-  for (int i = lane; i < t.n_slots; i += 32) {
+  for (int i = lane; i < t.n_slots; i += GW) {
     float* w = ws.sw + (size_t)i * kSlotF;
     fqmat(FQ{w[8], w[9], w[10], w[11]}, w + 16);
   }
@@ -440,9 +446,9 @@ struct CostArgs {
 
 // Cost of ws.q (returned on every lane) and, when WANT_GRAD, its gradient in ws.g.
 // target: 7 floats (x y z qx qy qz qw) or null.
-template <bool WANT_GRAD>
+template <bool WANT_GRAD, int GW = 32>
 __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const float* target, int lane) {
-  warp_fk(t, ws, lane);
+  warp_fk<GW>(t, ws, lane);
   // pose term (lane 0), wrench kept in misc[0..5]
   float cost = 0.f;
   if (lane == 0) {
@@ -469,7 +475,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
   int best_k = 0x7fffffff;
   float best_g[3] = {0.f, 0.f, 0.f};
   float hsum = 0.f;
-  for (int k = lane; k < t.n_sph; k += 32) {
+  for (int k = lane; k < t.n_sph; k += GW) {
     const GSph& s = t.sph[k];
     const float* w = ws.sw + (size_t)s.slot * kSlotF;
     const float* R = w + 16;
@@ -509,10 +515,10 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
   }
   if (a.mode == MODE_SUM) {
     cost += a.w_col * hsum;
-    cost = warp_sum(cost);
+    cost = warp_sum<GW>(cost);
   } else {
-    // warp argmin over (d, sphere index); ties go to the lower index
-    for (int o = 16; o > 0; o >>= 1) {
+    // the unit's argmin over (d, sphere index); ties go to the lower index
+    for (int o = GW / 2; o > 0; o >>= 1) {
       const float od = __shfl_xor_sync(0xffffffffu, best_d, o);
       const int ok = __shfl_xor_sync(0xffffffffu, best_k, o);
       if (od < best_d || (od == best_d && ok < best_k)) {
@@ -523,7 +529,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
     cost = fminf(best_d, a.cutoff);
     if (WANT_GRAD) {
       __syncwarp();
-      if (best_d < a.cutoff && (best_k & 31) == lane) {  // the owner seeds the adjoint with grad d
+      if (best_d < a.cutoff && (best_k & (GW - 1)) == lane) {  // the owner seeds the adjoint with grad d
         const GSph& s = t.sph[best_k];
         const float* w = ws.sw + (size_t)s.slot * kSlotF;
         const float* R = w + 16;
@@ -542,7 +548,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
   if (!WANT_GRAD) return cost;
   __syncwarp();
   // per-slot wrench (moment about the slot origin), plus the pose wrench
-  for (int i = lane; i < t.n_slots; i += 32) {
+  for (int i = lane; i < t.n_slots; i += GW) {
     float F[3] = {0.f, 0.f, 0.f}, M[3] = {0.f, 0.f, 0.f};
     for (int k = t.sbeg[i]; k < t.sbeg[i + 1]; k++) {
       const float* sa = ws.sadj + (size_t)6 * k;
@@ -563,7 +569,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
       w[28 + q] = M[q];
     }
   }
-  for (int j = lane; j < t.qd; j += 32) ws.g[j] = 0.f;
+  for (int j = lane; j < t.qd; j += GW) ws.g[j] = 0.f;
   __syncwarp();
   if (lane == 0) {  // children first: move each subtree wrench to the parent origin
     for (int i = t.n_slots - 1; i >= 0; i--) {
@@ -581,7 +587,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
     }
   }
   __syncwarp();
-  for (int i = lane; i < t.n_slots; i += 32) {
+  for (int i = lane; i < t.n_slots; i += GW) {
     const GSlot& s = t.slot[i];
     const float* w = ws.sw + (size_t)i * kSlotF;
     if (s.parent < 0) {
@@ -619,32 +625,45 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
 }
 
 // ---------------------------------------------------------------------------------- IK batch
-template <bool WANT_GRAD>
-__global__ void __launch_bounds__(kNW * 32) k_ik_cost(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, CostArgs a,
+// lanes per problem and the blocks per SM the registers are sized for: 16 lanes at 4 blocks of 256
+// threads (64 registers) keep all 8,192 problems of the 7-joint IK workload resident at once and
+// measured fastest, ahead of 16 lanes at 2 or 3 blocks and of a whole warp per problem
+constexpr int kIkGW = 16, kIkBlocksPerSm = 4;
+// GW lanes per problem, 32 / GW problems per warp (the FK composition and the wrench accumulation,
+// which run on one lane per problem, then serve that many problems at a time).  The loop over a
+// warp's problems runs the same number of times on every group of the warp; a group past the end
+// works on a copy of the last problem and writes nothing.
+template <bool WANT_GRAD, int GW>
+__global__ void __launch_bounds__(kNW * 32, kIkBlocksPerSm) k_ik_cost(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, CostArgs a,
                                                       Layout L, float* __restrict__ q, const float* __restrict__ target, int64_t B,
                                                       float* __restrict__ cost, float* __restrict__ grad, float* __restrict__ hist) {
   extern __shared__ __align__(16) char smem[];
   Tab t;
   stage(T, state, L, smem, t);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  WS ws = warp_ws(L, smem, w);
-  for (int64_t u = (int64_t)blockIdx.x * kNW + w; u < B; u += (int64_t)gridDim.x * kNW) {
-    for (int j = lane; j < a.qd; j += 32) ws.q[j] = q[u * a.qd + j];
+  constexpr int per_warp = 32 / GW, groups = kNW * per_warp;
+  const int lane = threadIdx.x & (GW - 1), gi = threadIdx.x / GW;
+  const int first = (threadIdx.x >> 5) * per_warp;  // the warp's first group
+  WS ws = warp_ws(L, smem, gi);
+  for (int64_t u0 = (int64_t)blockIdx.x * groups + first; u0 < B; u0 += (int64_t)gridDim.x * groups) {
+    const int64_t u_own = u0 + (gi - first);
+    const bool have = u_own < B;
+    const int64_t u = have ? u_own : B - 1;
+    for (int j = lane; j < a.qd; j += GW) ws.q[j] = q[u * a.qd + j];
     __syncwarp();
     const float* tg = target ? target + u * 7 : nullptr;
     if (a.steps <= 0) {  // one evaluation
-      const float c = warp_cost<WANT_GRAD>(t, a, ws, tg, lane);
-      if (lane == 0 && cost) cost[u] = c;
-      if (WANT_GRAD)
-        for (int j = lane; j < a.qd; j += 32) grad[u * a.qd + j] = ws.g[j];
+      const float c = warp_cost<WANT_GRAD, GW>(t, a, ws, tg, lane);
+      if (have && lane == 0 && cost) cost[u] = c;
+      if (WANT_GRAD && have)
+        for (int j = lane; j < a.qd; j += GW) grad[u * a.qd + j] = ws.g[j];
       __syncwarp();
       continue;
     }
     // gradient descent, all steps in registers/shared memory: q <- clamp(q - lr * grad)
     for (int it = 0; it < a.steps; it++) {
-      const float c = warp_cost<true>(t, a, ws, tg, lane);
-      if (lane == 0 && hist) hist[u * a.steps + it] = c;
-      for (int j = lane; j < a.qd; j += 32) {
+      const float c = warp_cost<true, GW>(t, a, ws, tg, lane);
+      if (have && lane == 0 && hist) hist[u * a.steps + it] = c;
+      for (int j = lane; j < a.qd; j += GW) {
         float v = fmaf(-a.lr, ws.g[j], ws.q[j]);
         if (a.clamp) v = fminf(fmaxf(v, a.lo[j]), a.hi[j]);
         ws.q[j] = v;
@@ -652,20 +671,24 @@ __global__ void __launch_bounds__(kNW * 32) k_ik_cost(const PmTablesHdr* __restr
       __syncwarp();
     }
     if (cost) {
-      const float c = warp_cost<false>(t, a, ws, tg, lane);
-      if (lane == 0) cost[u] = c;
+      const float c = warp_cost<false, GW>(t, a, ws, tg, lane);
+      if (have && lane == 0) cost[u] = c;
     }
-    for (int j = lane; j < a.qd; j += 32) q[u * a.qd + j] = ws.q[j];
+    if (have)
+      for (int j = lane; j < a.qd; j += GW) q[u * a.qd + j] = ws.q[j];
     __syncwarp();
   }
 }
 
 // -------------------------------------------------------------------------- trajectory batch
-// One warp per waypoint.  wp_cost[u] = collision hinge of waypoint u plus, for interior
-// waypoints, the smoothness term of its acceleration; grad row u when requested.
-// Up to 85 registers (3 blocks of 256 threads per SM): 4 % faster than the compiler's own choice for
-// this kernel; the IK kernel measured slower with any bound, so it keeps the default.
-template <bool WANT_GRAD>
+// lanes per waypoint: a whole warp measured 12 % faster than half warps on the 512-trajectory
+// planar-chain workload (the cloud queries of a half warp's spheres diverge more)
+constexpr int kTrajGW = 32;
+// GW lanes per waypoint: 32 (one waypoint per warp) or 16 (two per warp, a half each, as in
+// k_ik_cost).  wp_cost[u] = collision hinge of waypoint u plus, for interior waypoints, the
+// smoothness term of its acceleration; grad row u when requested.
+// Up to 85 registers (3 blocks of 256 threads per SM).
+template <bool WANT_GRAD, int GW>
 __global__ void __launch_bounds__(kNW * 32, 3) k_traj_cost(const PmTablesHdr* __restrict__ T, const double* __restrict__ state, CostArgs a,
                                                         Layout L, const float* __restrict__ q, const int64_t* __restrict__ off,
                                                         int64_t n_traj, int64_t n_wp, float* __restrict__ wp_cost,
@@ -673,10 +696,15 @@ __global__ void __launch_bounds__(kNW * 32, 3) k_traj_cost(const PmTablesHdr* __
   extern __shared__ __align__(16) char smem[];
   Tab t;
   stage(T, state, L, smem, t);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  WS ws = warp_ws(L, smem, w);
+  constexpr int per_warp = 32 / GW, groups = kNW * per_warp;
+  const int lane = threadIdx.x & (GW - 1), gi = threadIdx.x / GW;
+  const int first = (threadIdx.x >> 5) * per_warp;
+  WS ws = warp_ws(L, smem, gi);
   const int d = a.qd;
-  for (int64_t u = (int64_t)blockIdx.x * kNW + w; u < n_wp; u += (int64_t)gridDim.x * kNW) {
+  for (int64_t u0 = (int64_t)blockIdx.x * groups + first; u0 < n_wp; u0 += (int64_t)gridDim.x * groups) {
+    const int64_t u_own = u0 + (gi - first);
+    const bool have = u_own < n_wp;  // a half past the end works on a copy of the last waypoint, writes nothing
+    const int64_t u = have ? u_own : n_wp - 1;
     // trajectory of u: the last i with off[i] <= u
     int64_t lo = 0, hi = n_traj;
     while (hi - lo > 1) {
@@ -685,25 +713,25 @@ __global__ void __launch_bounds__(kNW * 32, 3) k_traj_cost(const PmTablesHdr* __
       else hi = mid;
     }
     const int64_t b = clamp_wp(off[lo], 0, n_wp), e = clamp_wp(off[lo + 1], b, n_wp);
-    for (int j = lane; j < d; j += 32) ws.q[j] = q[u * d + j];
+    for (int j = lane; j < d; j += GW) ws.q[j] = q[u * d + j];
     __syncwarp();
-    float c = warp_cost<WANT_GRAD>(t, a, ws, nullptr, lane);
+    float c = warp_cost<WANT_GRAD, GW>(t, a, ws, nullptr, lane);
     // smoothness: acc(k) = q[k+1] - 2 q[k] + q[k-1] for b < k < e-1
     auto acc = [&](int64_t k, int j) -> float {
       if (k <= b || k >= e - 1) return 0.f;
       return q[(k + 1) * d + j] - 2.f * q[k * d + j] + q[(k - 1) * d + j];
     };
     float sm = 0.f;
-    for (int j = lane; j < d; j += 32) {
+    for (int j = lane; j < d; j += GW) {
       const float ac = acc(u, j);
       sm = fmaf(a.dofw2[j] * ac, ac, sm);
-      if (WANT_GRAD) {
+      if (WANT_GRAD && have) {
         const float gs = 2.f * a.w_smooth * a.dofw2[j] * (acc(u - 1, j) - 2.f * ac + acc(u + 1, j));
         grad[u * d + j] = ws.g[j] + gs;
       }
     }
-    c += a.w_smooth * warp_sum(sm);
-    if (lane == 0) wp_cost[u] = c;
+    c += a.w_smooth * warp_sum<GW>(sm);
+    if (have && lane == 0) wp_cost[u] = c;
     __syncwarp();
   }
 }
@@ -764,12 +792,12 @@ CostArgs to_args(const pmg::GradArgs& g, int qd) {
   return a;
 }
 
-int grid_for(const void* fn, size_t smem, int64_t units) {
+int grid_for(const void* fn, size_t smem, int64_t units, int per_block = kNW) {
   int dev = 0, n_sm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kNW * 32, smem);
-  const int64_t need = (units + kNW - 1) / kNW;
+  const int64_t need = (units + per_block - 1) / per_block;
   return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)std::max(per_sm, 1) * n_sm));
 }
 
@@ -791,20 +819,21 @@ size_t grad_smem_bytes(const PmTablesHdr& h) { return make_layout(h.n_slots, h.n
 cudaError_t launch_ik_cost(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const GradArgs& g, float* q,
                            const float* target, int64_t B, float* cost, float* grad, float* hist, cudaStream_t s) {
   if (B <= 0) return cudaSuccess;
-  const Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim);
+  constexpr int GW = kIkGW, groups = kNW * (32 / GW);
+  const Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim, groups);
   const CostArgs a = to_args(g, h.q_dim);
   if (grad || g.steps > 0) {
-    auto fn = k_ik_cost<true>;
+    auto fn = k_ik_cost<true, GW>;
     cudaError_t e = prep(fn, L.total);
     if (e != cudaSuccess) return e;
     prof_begin("k_ik_cost", s);
-    fn<<<grid_for((const void*)fn, L.total, B), kNW * 32, L.total, s>>>(T, state, a, L, q, target, B, cost, grad, hist);
+    fn<<<grid_for((const void*)fn, L.total, B, groups), kNW * 32, L.total, s>>>(T, state, a, L, q, target, B, cost, grad, hist);
     prof_end("k_ik_cost", s);
   } else {
-    auto fn = k_ik_cost<false>;
+    auto fn = k_ik_cost<false, GW>;
     cudaError_t e = prep(fn, L.total);
     if (e != cudaSuccess) return e;
-    fn<<<grid_for((const void*)fn, L.total, B), kNW * 32, L.total, s>>>(T, state, a, L, q, target, B, cost, nullptr, nullptr);
+    fn<<<grid_for((const void*)fn, L.total, B, groups), kNW * 32, L.total, s>>>(T, state, a, L, q, target, B, cost, nullptr, nullptr);
   }
   return cudaGetLastError();
 }
@@ -813,21 +842,22 @@ cudaError_t launch_traj_cost(const PmTablesHdr* T, const PmTablesHdr& h, const d
                              const int64_t* off, int64_t n_traj, int64_t n_wp, float* wp_cost, float* cost, float* grad,
                              cudaStream_t s) {
   if (n_traj <= 0) return cudaSuccess;
-  const Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim);
+  constexpr int GW = kTrajGW, groups = kNW * (32 / GW);
+  const Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim, groups);
   const CostArgs a = to_args(g, h.q_dim);
   if (n_wp > 0) {
     if (grad) {
-      auto fn = k_traj_cost<true>;
+      auto fn = k_traj_cost<true, GW>;
       cudaError_t e = prep(fn, L.total);
       if (e != cudaSuccess) return e;
       prof_begin("k_traj_cost", s);
-      fn<<<grid_for((const void*)fn, L.total, n_wp), kNW * 32, L.total, s>>>(T, state, a, L, q, off, n_traj, n_wp, wp_cost, grad);
+      fn<<<grid_for((const void*)fn, L.total, n_wp, groups), kNW * 32, L.total, s>>>(T, state, a, L, q, off, n_traj, n_wp, wp_cost, grad);
       prof_end("k_traj_cost", s);
     } else {
-      auto fn = k_traj_cost<false>;
+      auto fn = k_traj_cost<false, GW>;
       cudaError_t e = prep(fn, L.total);
       if (e != cudaSuccess) return e;
-      fn<<<grid_for((const void*)fn, L.total, n_wp), kNW * 32, L.total, s>>>(T, state, a, L, q, off, n_traj, n_wp, wp_cost, nullptr);
+      fn<<<grid_for((const void*)fn, L.total, n_wp, groups), kNW * 32, L.total, s>>>(T, state, a, L, q, off, n_traj, n_wp, wp_cost, nullptr);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
