@@ -354,6 +354,16 @@ def bench_chain7(dev, timed):
         ms_e_graph = timed(eg.replay, 10)
     except Exception:  # noqa: BLE001 - reported as null
         ms_e_graph = None
+    # the composite (IneqCompositeCst) of the collision constraint and an end-link height bound:
+    # one fused launch vs the members one after the other (fast collision path, plain bound)
+    from plainmp_gb300 import BaseType, IneqCompositeCst, LinkPositionBoundCst
+
+    bound = LinkPositionBoundCst(cst.get_kin(), robot.control_joints, BaseType.FIXED, robot.end_link, 2, lb=0.0)
+    comp = IneqCompositeCst([cst, bound])
+    cout = torch.empty(Q.shape[0], dtype=torch.uint8, device=dev)
+    ms_c_fused = timed(lambda: comp.is_valid_fast(Q, out=cout), 10)
+    ms_c_members = timed(lambda: cst.is_valid_fast(Q) & bound.is_valid_batch(Q), 10)
+    same_c = bool(torch.equal(comp.is_valid_fast(Q), cst.is_valid_batch(Q) & bound.is_valid_batch(Q)))
     return {
         "C0": {"workload": "7-joint chain, 56 spheres, 10 boxes + 5 spheres + 5 cylinders, 4096 configurations",
                "unit": "configs/s", "plain_fp64": 4096 / (ms_plain / 1e3), "fast_with_distances": 4096 / (ms_fast / 1e3),
@@ -366,6 +376,10 @@ def bench_chain7(dev, timed):
                "effective": {"kflop_per_config": C0_FLOP / 1e3,
                              "fast_tflops": 4096 / (ms_fast / 1e3) * C0_FLOP / 1e12,
                              "plain_tflops": 4096 / (ms_plain / 1e3) * C0_FLOP / 1e12}},
+        "C0_composite": {"workload": "the C0 batch against IneqCompositeCst([collision, end-link z >= 0])", "unit": "configs/s",
+                         "fused": 4096 / (ms_c_fused / 1e3), "members_in_turn": 4096 / (ms_c_members / 1e3),
+                         "ms": {"fused": ms_c_fused, "members_in_turn": ms_c_members}, "validity_identical": same_c,
+                         "valid_fraction": float(comp.is_valid_fast(Q).float().mean())},
         "C1": {"workload": "1024 straight edges on the C0 chain and scene, box validator width 0.05 rad, 1-120 waypoints",
                "unit": "edges/s", "plain_fp64": 1024 / (ms_e_plain / 1e3), "fast_persistent": 1024 / (ms_e_fast / 1e3),
                "fast_cuda_graph": 1024 / (ms_e_graph / 1e3) if ms_e_graph else None,

@@ -253,6 +253,29 @@ int pmgpu_posecst_evaluate(pmgpu_posecst* c, const double* q, int64_t B, double*
  * is_valid_dirty); an equality constraint gives PMGPU_ERR_INVALID. */
 int pmgpu_posecst_is_valid(pmgpu_posecst* c, const double* q, int64_t B, uint8_t* out, int mem, void* stream);
 
+/* ---------------------------------------------------------------- composite constraint
+ * IneqCompositeCst::is_valid (constraints/composite_constraint.hpp:98-105; bindings/constraint.cpp:
+ * 105-112) of the collision constraint c and the LinkPositionBoundCst handles bounds[0..n_bounds)
+ * (primitive_link_position_bound.cpp:69-79), in one fast launch: the bounds are decided on the
+ * same FP32 FK as c's sphere terms, an undecided one by the FP64 recheck, so the FK runs once per
+ * configuration (the reference's one update_kintree(q, false)).  Same booleans as the AND of
+ * pmgpu_cst_is_valid and pmgpu_posecst_is_valid.  Every bound must be made on c's kinematic model
+ * with c's control joints and base type (else PMGPU_ERR_RUNTIME "All constraints must have the
+ * same kinematic chain" or PMGPU_ERR_INVALID); a LinkPoseCst handle gives PMGPU_ERR_INVALID.  A
+ * bound's link joins c's FK slots if no sphere chain reaches it.  stats as pmgpu_cst_is_valid_fast.
+ * No counterpart entry point in the reference, whose composite is a C++ class. */
+int pmgpu_composite_is_valid_fast(pmgpu_cst* c, pmgpu_posecst* const* bounds, int n_bounds, const double* q, int64_t B,
+                                  uint8_t* out, int64_t* stats, int mem, void* stream);
+/* checkMotion (ompl/motion_validator.cpp:17-79) with the composite's is_valid at every checked
+ * waypoint: the constraint CollisionAwareSpaceInformation checks (ompl/ompl_thin_wrap.hpp:114-120)
+ * is the problem's global inequality constraint, a composite in general
+ * (src/plainmp/ompl_solver.py:250-257; simplify_path takes an IneqCompositeCst, :285-289).
+ * Arguments as pmgpu_check_motion_fast and
+ * pmgpu_composite_is_valid_fast. */
+int pmgpu_composite_check_motion_fast(pmgpu_cst* c, pmgpu_posecst* const* bounds, int n_bounds, const double* s1, const double* s2,
+                                      int64_t E, int validator_type, const double* width, double resolution, uint8_t* out,
+                                      int64_t* stats, int mem, void* stream);
+
 /* ---------------------------------------------------------------- link poses
  * World pose (x y z qx qy qz qw) of `link` for B configurations, FP64, the FK of
  * ConstraintBase::update_kintree with std::sin/std::cos (constraints/primitive.hpp:38-62)

@@ -114,6 +114,8 @@ _SIGS = {
     "pmgpu_posecst_update_kintree": (_i, [_p, _dp, _i]),
     "pmgpu_posecst_evaluate": (_i, [_p, _p, _i64, _p, _p, _i, _p]),
     "pmgpu_posecst_is_valid": (_i, [_p, _p, _i64, _p, _i, _p]),
+    "pmgpu_composite_is_valid_fast": (_i, [_p, _p, _i, _p, _i64, _p, _p, _i, _p]),
+    "pmgpu_composite_check_motion_fast": (_i, [_p, _p, _i, _p, _p, _i64, _i, _p, _d, _p, _p, _i, _p]),
     "pmgpu_ik_cost": (_i, [_p, _p, _p, _p, _i64, _p, _p, _i, _p]),
     "pmgpu_ik_descend": (_i, [_p, _p, _p, _p, _i64, C.c_int32, C.c_float, C.c_int32, _p, _p, _i, _p]),
     "pmgpu_traj_cost": (_i, [_p, _p, _p, _p, _i64, _i64, _p, _p, _i, _p]),

@@ -405,9 +405,43 @@ class IneqCompositeCst(_CompositeBase):
 
     _member = IneqConstraintBase
 
+    def fused_parts(self):
+        """(collision constraint, [bounds]) when the members are one SphereCollisionCst and any
+        number of LinkPositionBoundCst: the fast path then checks all of them in one launch on one
+        FK (pmgpu_composite_is_valid_fast); else None."""
+        sph = [c for c in self.constraints if isinstance(c, SphereCollisionCst)]
+        bnd = [c for c in self.constraints if isinstance(c, LinkPositionBoundCst)]
+        if len(sph) != 1 or len(sph) + len(bnd) != len(self.constraints):
+            return None
+        return sph[0], bnd
+
+    def is_valid_fast(self, Q, stats: bool = False, out=None):
+        """Fused FP32 + FP64-recheck check of a SphereCollisionCst and LinkPositionBoundCst members
+        (fused_parts): (B,) uint8 identical to the AND of the members' plain checks; stats as
+        SphereCollisionCst.is_valid_fast."""
+        parts = self.fused_parts()
+        if parts is None:
+            raise TypeError("is_valid_fast needs one SphereCollisionCst and LinkPositionBoundCst members")
+        sph, bnd = parts
+        b = sph._batch(Q)
+        if out is not None:
+            optr = b.out(out, (b.shape[0],), np.uint8)
+        else:
+            out, optr = b.empty((b.shape[0],), np.uint8)
+        hs = (C.c_void_p * max(len(bnd), 1))(*[c._h for c in bnd])
+        st = np.zeros(4, dtype=np.int64)
+        check(lib.pmgpu_composite_is_valid_fast(sph._h, hs, len(bnd), b.ptr, b.shape[0], optr,
+                                                C.c_void_p(st.ctypes.data) if stats else None, b.mem, b.stream))
+        if stats:
+            return out, {"configs": int(st[0]), "rechecked_terms": int(st[1]), "rechecked_configs": int(st[2])}
+        return out
+
     def is_valid_batch(self, Q, fast: bool = True):
-        """(B,) uint8 AND of the members' validity; SphereCollisionCst members use the FP32 +
-        FP64-recheck path when fast (same booleans), else the plain FP64 method."""
+        """(B,) uint8 AND of the members' validity.  fast: one fused launch when fused_parts
+        applies (same booleans), else each SphereCollisionCst member on its FP32 + FP64-recheck
+        path; not fast: every member's plain FP64 method."""
+        if fast and self.fused_parts() is not None:
+            return self.is_valid_fast(Q)
         ok = None
         for c in self.constraints:
             if isinstance(c, SphereCollisionCst):

@@ -686,6 +686,8 @@ struct HostCst {
   DevBuf g_wp;                        // trajectory costs: per-waypoint partial costs
   std::vector<int16_t> seq_host;
   std::vector<int> extra_links;  // links a pose term needs that no sphere chain reaches
+  DevBuf d_bnd;                       // a composite call's link-position bounds, as last uploaded
+  std::vector<PmPoseTerm> bnd_up;     // their host copy (re-uploaded when they change)
 
   // FK slot of `link`; the link (and its ancestors) joins the tables if it is not there yet.
   int slot_for_link(int link) {
@@ -1846,7 +1848,7 @@ static unsigned hard_query_cap(int64_t B, int64_t ns) {
 // Host-memory fast call of a large batch, in up to 8 chunks of at least 8,192 configurations on two
 // streams (FastPipe).  Every configuration is independent, so the outcome is the same as one launch.
 static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* st, const double* q, int64_t B, uint8_t* out,
-                                float* dist32, int64_t* stats, cudaStream_t s) {
+                                float* dist32, int64_t* stats, cudaStream_t s, PmLinkBounds bnd) {
   FastPipe& P = C.pipe;
   P.init();
   const int64_t d = C.q_dim(), ns = C.n_spheres();
@@ -1882,7 +1884,7 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
     char* cc = ctl + i * 64;
     cuda_check(launch_fast_valid(T, C.hdr, st, din[k], n, dout[k], ddist[k], 0.1f, items[k], (unsigned int*)cc, cap, ovf + c0,
                                  (unsigned long long*)(cc + 16), C.fast_cpb, C.fast_nt, cs, hqb[k], (unsigned long long*)(cc + 48), hq_cap,
-                                 C.tune),
+                                 C.tune, bnd),
                "is_valid_fast");
     cuda_check(cudaMemcpyAsync(out + c0, dout[k], (size_t)n, cudaMemcpyDeviceToHost, cs), "D2H copy");
     if (dist32) cuda_check(cudaMemcpyAsync(dist32 + c0 * ns, ddist[k], (size_t)(n * ns) * 4, cudaMemcpyDeviceToHost, cs), "D2H copy");
@@ -1902,8 +1904,9 @@ static void fast_host_pipelined(HostCst& C, const PmTablesHdr* T, const double* 
   }
 }
 
-int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats, int mem,
-                            void* stream) {
+// pmgpu_cst_is_valid_fast, and with link-position bounds the fused composite check
+static int fast_valid_entry(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats, int mem,
+                            void* stream, PmLinkBounds bnd) {
   return guarded([&] {
     check_ptr(c, "cst");
     check_mem(mem);
@@ -1917,7 +1920,7 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     const double* st = C.kin->d_state.as<double>();
     cudaStream_t s = as_stream(stream);
     if (mem == PMGPU_MEM_HOST && B >= 16384) {
-      fast_host_pipelined(C, T, st, q, B, out, dist32, stats, s);
+      fast_host_pipelined(C, T, st, q, B, out, dist32, stats, s, bnd);
       return;
     }
     const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(4 * B, 1 << 16), (int64_t)1 << 28);
@@ -1946,7 +1949,7 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
     const unsigned hq_cap = hard_query_cap(B, C.n_spheres());
     void* hq = dd ? C.f_hq.ensure((size_t)hq_cap * 32) : nullptr;
     cuda_check(launch_fast_valid(T, C.hdr, st, dq, B, dout, dd, 0.1f, items, count, cap, ovf, dstats, C.fast_cpb, C.fast_nt, s, hq,
-                                 (unsigned long long*)(ctl + 48), hq_cap, C.tune),
+                                 (unsigned long long*)(ctl + 48), hq_cap, C.tune, bnd),
                "is_valid_fast");
     char* pin_out = pin ? pin + up16(nq) : nullptr;
     char* pin_dist = pin ? pin_out + up16((size_t)B) : nullptr;
@@ -1971,6 +1974,10 @@ int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* o
       }
     }
   });
+}
+int pmgpu_cst_is_valid_fast(pmgpu_cst* c, const double* q, int64_t B, uint8_t* out, float* dist32, int64_t* stats, int mem,
+                            void* stream) {
+  return fast_valid_entry(c, q, B, out, dist32, stats, mem, stream, PmLinkBounds{nullptr, 0});
 }
 int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
                        double resolution, uint8_t* out, int64_t* n_checked, int mem, void* stream) {
@@ -2022,8 +2029,9 @@ int pmgpu_check_motion(pmgpu_cst* c, const double* s1, const double* s2, int64_t
   });
 }
 
-int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
-                            double resolution, uint8_t* out, int64_t* stats, int mem, void* stream) {
+// pmgpu_check_motion_fast, and with link-position bounds the fused composite check
+static int fast_edges_entry(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
+                            double resolution, uint8_t* out, int64_t* stats, int mem, void* stream, PmLinkBounds bnd) {
   return guarded([&] {
     check_ptr(c, "cst");
     check_mem(mem);
@@ -2090,7 +2098,7 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
     int n_sm = 0;
     cuda_check(sm_count(&n_sm), "device attribute");
     cuda_check(launch_fast_edges(T, C.hdr, st, d1, d2, E, validator_type, dw, resolution, seq, sr, n, off, next, dout, items, count, cap,
-                                 ovf, dstats, C.edge_cpb, C.edge_nt, n_sm, s),
+                                 ovf, dstats, C.edge_cpb, C.edge_nt, n_sm, s, bnd),
                "check_motion_fast");
     char* pin_out = pin ? pin + 2 * up16(ns_) + up16(nw) : nullptr;
     if (mem == PMGPU_MEM_HOST && E) cuda_check(cudaMemcpyAsync(pin_out, dout, (size_t)E, cudaMemcpyDeviceToHost, s), "D2H copy");
@@ -2116,6 +2124,11 @@ int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, in
       }
     }
   });
+}
+
+int pmgpu_check_motion_fast(pmgpu_cst* c, const double* s1, const double* s2, int64_t E, int validator_type, const double* width,
+                            double resolution, uint8_t* out, int64_t* stats, int mem, void* stream) {
+  return fast_edges_entry(c, s1, s2, E, validator_type, width, resolution, out, stats, mem, stream, PmLinkBounds{nullptr, 0});
 }
 
 // ------------------------------------------------------------------ link poses, differentiable costs
@@ -2370,6 +2383,71 @@ int pmgpu_linkbound_create(pmgpu_model* kin, const char* const* control_joints, 
 }
 
 void pmgpu_posecst_destroy(pmgpu_posecst* c) { delete c; }
+
+// ------------------------------------------------------------------ composite (IneqCompositeCst)
+}  // extern "C"
+namespace {
+// The link-position bounds of `bounds` as device terms on c's tables: every handle must be a
+// LinkPositionBoundCst on c's kinematic model with c's control joints and base type (the
+// composite's members share one update_kintree, composite_constraint.hpp:27-37, 98-105).  A
+// bound's link joins c's FK slots if no sphere chain reaches it.
+PmLinkBounds composite_bounds(HostCst& C, pmgpu_posecst* const* bounds, int n_bounds, cudaStream_t s) {
+  if (n_bounds < 0) throw std::invalid_argument("negative bound count");
+  if (n_bounds > 0) check_ptr(bounds, "bounds");
+  std::vector<std::pair<int, PmPoseTerm>> terms;
+  for (int i = 0; i < n_bounds; i++) {
+    const pmgpu_posecst* b = bounds[i];
+    check_ptr(b, "bound");
+    if (b->equality) fail(PMGPU_ERR_INVALID, "composite is_valid: members must be inequality constraints (LinkPositionBoundCst)");
+    if (b->c.kin.get() != C.kin.get()) fail(PMGPU_ERR_RUNTIME, "All constraints must have the same kinematic chain");
+    if (b->c.ids != C.ids || b->c.base_type != C.base_type)
+      fail(PMGPU_ERR_INVALID, "composite is_valid: members need the same control joints and base type");
+    for (size_t j = 0; j < b->terms.size(); j++) {
+      if (b->terms[j].kind != PM_TERM_POSITION_BOUND) fail(PMGPU_ERR_INVALID, "composite is_valid: not a link-position bound");
+      terms.push_back({b->links[j], b->terms[j]});
+    }
+  }
+  if (terms.empty()) return PmLinkBounds{nullptr, 0};
+  if (terms.size() > 4096) fail(PMGPU_ERR_INVALID, "composite is_valid: at most 4096 link-position bounds");
+  for (auto& t : terms) C.slot_for_link(t.first);  // first every link joins the tables, then the slots are final
+  C.tables();
+  std::vector<PmPoseTerm> up;
+  for (auto& t : terms) {
+    PmPoseTerm x = t.second;
+    x.slot = C.slot_of_link[t.first];
+    up.push_back(x);
+  }
+  const size_t bytes = up.size() * sizeof(PmPoseTerm);
+  if (!C.d_bnd.p || up.size() != C.bnd_up.size() || std::memcmp(up.data(), C.bnd_up.data(), bytes) != 0) {
+    C.bnd_up = up;  // the copy's source stays alive until the next change
+    cuda_check(cudaMemcpyAsync(C.d_bnd.ensure(bytes), C.bnd_up.data(), bytes, cudaMemcpyHostToDevice, s), "bounds upload");
+  }
+  return PmLinkBounds{C.d_bnd.as<PmPoseTerm>(), (int32_t)up.size()};
+}
+}  // namespace
+extern "C" {
+
+int pmgpu_composite_is_valid_fast(pmgpu_cst* c, pmgpu_posecst* const* bounds, int n_bounds, const double* q, int64_t B,
+                                  uint8_t* out, int64_t* stats, int mem, void* stream) {
+  PmLinkBounds bnd{nullptr, 0};
+  const int rc = guarded([&] {
+    check_ptr(c, "cst");
+    bnd = composite_bounds(c->c, bounds, n_bounds, as_stream(stream));
+  });
+  if (rc != PMGPU_OK) return rc;
+  return fast_valid_entry(c, q, B, out, nullptr, stats, mem, stream, bnd);
+}
+int pmgpu_composite_check_motion_fast(pmgpu_cst* c, pmgpu_posecst* const* bounds, int n_bounds, const double* s1, const double* s2,
+                                      int64_t E, int validator_type, const double* width, double resolution, uint8_t* out,
+                                      int64_t* stats, int mem, void* stream) {
+  PmLinkBounds bnd{nullptr, 0};
+  const int rc = guarded([&] {
+    check_ptr(c, "cst");
+    bnd = composite_bounds(c->c, bounds, n_bounds, as_stream(stream));
+  });
+  if (rc != PMGPU_OK) return rc;
+  return fast_edges_entry(c, s1, s2, E, validator_type, width, resolution, out, stats, mem, stream, bnd);
+}
 
 int pmgpu_posecst_dims(const pmgpu_posecst* c, int* q_dim, int* cst_dim, int* is_equality) {
   return guarded([&] {

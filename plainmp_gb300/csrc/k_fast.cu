@@ -96,6 +96,7 @@ struct Scratch {
   unsigned int hq_cap;
   int st_log2;             // sphere tile: log2 of the spheres a warp row of sphere tasks holds (0: the
                            // least, 32 / configurations per block)
+  PmLinkBounds bnd = PmLinkBounds{nullptr, 0};  // a composite constraint's link-position bounds
 };
 
 __device__ __forceinline__ float3 xf(const float* P, float x, float y, float z) {  // R (row-major 9) * v + t (P[9..11])
@@ -893,6 +894,7 @@ struct CfgSource {  // a batch of configurations q[B x q_dim]
   const double* q;
   int64_t B;
   uint8_t* out;
+  PmLinkBounds bnd;  // link-position bounds checked with the collision terms (composite constraint)
   __device__ const double* cfg(const PmTablesHdr* T, int64_t i, double*) const { return q + i * T->q_dim; }
   __device__ bool pre_skip(int64_t) const { return false; }     // before the fast pass: nothing known
   __device__ bool skip(int64_t i) const { return out[i] == 0; }  // after it: already invalid
@@ -901,7 +903,7 @@ struct CfgSource {  // a batch of configurations q[B x q_dim]
   __device__ int64_t overflow_slot(int64_t i) const { return i; }
   __device__ int64_t n_overflow_slots() const { return B; }
   __device__ void full_check(const TView& v, const double* state, int64_t i, double*) const {
-    out[i] = is_valid_cfg(v, state, q + i * v.T->q_dim) ? 1 : 0;
+    out[i] = is_valid_cfg(v, state, q + i * v.T->q_dim, bnd) ? 1 : 0;
   }
 };
 
@@ -917,6 +919,7 @@ struct EdgeSource {
   const int16_t* seq;
   int64_t E;
   uint8_t* valid;  // per edge, 1 until a waypoint is found colliding
+  PmLinkBounds bnd;  // link-position bounds checked at every waypoint (composite constraint)
   __device__ int64_t edge_of(int64_t w) const {
     int64_t lo = 0, hi = E - 1;
     while (lo < hi) {
@@ -954,7 +957,7 @@ struct EdgeSource {
   // every waypoint of edge e in the plain FP64 method
   __device__ void full_check(const TView& v, const double* state, int64_t e, double* buf) const {
     bool ok = true;
-    for (int64_t w = off[e]; w < off[e] + n[e] && ok; w++) ok = is_valid_cfg(v, state, cfg(v.T, w, buf));
+    for (int64_t w = off[e]; w < off[e] + n[e] && ok; w++) ok = is_valid_cfg(v, state, cfg(v.T, w, buf), bnd);
     if (!ok) valid[e] = 0;
   }
 };
@@ -1007,6 +1010,23 @@ __device__ void fast_block(const TView& v, const Smem& sm, const double* __restr
   }
   __syncthreads();
   const bool want_dist = dist32 != nullptr;
+  // ---- 1b. link-position bounds of a composite constraint (LinkPositionBoundCst::is_valid_dirty,
+  //          primitive_link_position_bound.cpp:69-79): the link's FP32 world position and its FK
+  //          error bound decide; an undecided bound goes to the FP64 recheck.  A failed bound marks
+  //          the configuration before the sphere tasks, which then skip it (validity mode).
+  for (int t = tid, nb = src.bnd.n; t < ncfg * nb; t += blockDim.x) {
+    const int c = t / nb, k = t - c * nb;
+    if (sm.flags[c] & 2) continue;
+    const PmPoseTerm& b = src.bnd.t[k];
+    const float* P = sm.pose + ((size_t)c * nsl + b.slot) * kPoseF;
+    const float x = P[9 + b.axis];
+    const float lo = (float)b.lb, hi = (float)b.ub;
+    // the FK error bound, plus the rounding of the bounds to FP32 and of the comparison
+    const float m = P[12] + margin32(fabsf(x) + (b.has_lb ? fabsf(lo) : 0.f) + (b.has_ub ? fabsf(hi) : 0.f));
+    const bool fail = (b.has_lb && x + m < lo) || (b.has_ub && x - m > hi);
+    if (fail) atomicOr(&sm.flags[c], FLAG_FAIL);
+    else if ((b.has_lb && x - m <= lo) || (b.has_ub && x + m >= hi)) push_item(scr, src, c0 + c, -1 - k, 0, 0);
+  }
   // ---- 2. group culling against each primitive
   for (int t = tid; t < ncfg * ng; t += blockDim.x) {
     const int c = t / ng, gi = t - c * ng;
@@ -1466,7 +1486,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 64)) k_fast_valid(const PmTa
   TView v(T);
   Smem sm = carve(smem_raw, T, CPB);
   stage_tables(v, sm, state);
-  CfgSource src{q, B, out};
+  CfgSource src{q, B, out, scr.bnd};
   const int64_t c0 = (int64_t)blockIdx.x * CPB;
   fast_block<CPB>(v, sm, state, src, c0, (int)(B - c0 < CPB ? B - c0 : CPB), dist32, cutoff, scr, sm.qbuf);
 }
@@ -1603,7 +1623,14 @@ __global__ void k_fast_recheck(const PmTablesHdr* __restrict__ T, const double* 
     const int4 it = scr.items[i];
     if (__shfl_sync(FULL, src.skip(it.x) ? 1 : 0, 0)) continue;
     bool hit = false;
-    if ((it.y & 1) == 0) {  // sphere it.z vs primitive it.y >> 1: gate AND test
+    if (it.y < 0) {  // link-position bound -1 - it.y of a composite constraint, in FP64 (every lane)
+      const PmPoseTerm& b = src.bnd.t[-1 - it.y];
+      DPose pose[PM_MAX_SLOTS];
+      fk64_need_warp(T, state, src.cfg(T, it.x, qbuf), T->base_type == PM_BASE_FIXED, slot_chain(T, b.slot), pose);
+      const D3& p = pose[b.slot].t;
+      const double x = b.axis == 0 ? p.x : (b.axis == 1 ? p.y : p.z);
+      hit = (b.has_lb && x < b.lb) || (b.has_ub && x > b.ub);
+    } else if ((it.y & 1) == 0) {  // sphere it.z vs primitive it.y >> 1: gate AND test
       const PmPrim& P = v.P[it.y >> 1];
       const PmGroup& g = v.G[v.sgroup[it.z]];
       // the FP64 FK of the slot's chain of ancestors, by the whole warp (every lane gets the poses)
@@ -1825,13 +1852,13 @@ static unsigned recheck_grid(int64_t units, int per_block, int n_sm) {
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq,
-                              unsigned long long* hq_count, unsigned int hq_cap, const FastTuning& tune) {
+                              unsigned long long* hq_count, unsigned int hq_cap, const FastTuning& tune, PmLinkBounds bnd) {
   if (B <= 0) return cudaSuccess;
   if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   // (hard-query entries hold 32-bit configuration indices)
   const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
-              split ? hq_cap : 0u, tune.sphere_tile_log2};
+              split ? hq_cap : 0u, tune.sphere_tile_log2, bnd};
   size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   unsigned grid = (unsigned)((B + cpb - 1) / cpb);
@@ -1856,7 +1883,7 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if (!launched) return cudaErrorInvalidValue;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   prof_end("k_fast_valid", s);
-  CfgSource src{q, B, out};
+  CfgSource src{q, B, out, bnd};
   int n_sm = 0;
   if ((e = sm_count(&n_sm)) != cudaSuccess) return e;
   if (split) {
@@ -1877,7 +1904,8 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
 cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
                               int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,
                               int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
-                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int nt, int n_sm, cudaStream_t s) {
+                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int nt, int n_sm, cudaStream_t s,
+                              PmLinkBounds bnd) {
   if (E <= 0) return cudaSuccess;
   if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   Scratch scr{items, count, cap, overflow, stats};
@@ -1886,7 +1914,7 @@ cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if (e != cudaSuccess) return e;
   k_scan1<<<1, 1024, 0, s>>>(n, E, off);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  EdgeSource src{s1, s2, off, n, sr, seq, E, out};
+  EdgeSource src{s1, s2, off, n, sr, seq, E, out, bnd};
   size_t sm = fast_smem_bytes(h, cpb, false);
   if (sm > 200 * 1024) return cudaErrorInvalidConfiguration;
   bool launched = false;

@@ -37,9 +37,10 @@ struct GSlot {
   float lq[4];  // REV: joint origin rotation; STATE: the fixed local rotation
   float lt[3];  // joint origin / fixed local translation
 };
-struct GSph {
+struct alignas(16) GSph {  // 32 bytes: one 16-byte and one 8-byte shared-memory load per sphere
   float x, y, z, r;
   int slot, active;  // active: takes part in the ext cost (its group is not self-only)
+  int pad0, pad1;
 };
 struct GPrim {
   int kind, aa, cloud, pad;
@@ -47,7 +48,7 @@ struct GPrim {
   float rot[9];
   float a, b, c, pad2;
 };
-constexpr int kSlotF = 32;  // floats of per-warp work per slot
+constexpr int kSlotF = 33;  // floats of per-unit work per slot (odd: lanes on different slots use different banks)
 
 struct Layout {
   int n_slots, n_sph, n_prims, qd, qpad;

@@ -137,6 +137,15 @@ struct PmPoseTerm {
   double lb, ub;
 };
 
+// Link-position bounds of an IneqCompositeCst (constraints/composite_constraint.hpp:98-105) made of
+// a SphereCollisionCst and LinkPositionBoundCst members, checked by the fast kernels on the
+// collision constraint's FK: n device terms of kind PM_TERM_POSITION_BOUND whose slots index the
+// collision constraint's tables.
+struct PmLinkBounds {
+  const PmPoseTerm* t;
+  int32_t n;
+};
+
 struct PmTablesHdr {
   int32_t n_slots, n_ctrl, n_groups, n_spheres;
   int32_t n_pairs, n_prims, q_dim, base_type;

@@ -51,17 +51,20 @@ struct FastTuning {
   int sphere_tile_log2 = 0;  // log2 of the spheres per warp row of sphere tasks (0: the least for the shape)
   int hq_blocks_per_sm = 4;  // k_hard_queries: blocks of 256 threads per SM
 };
+// bnd: link-position bounds of a composite constraint, decided in the same kernels (none by default).
 // hq (hq_cap 32-byte entries) and hq_count (zeroed by the caller): with distances, the hard cloud
 // queries are answered by a second kernel over this global queue; null keeps them in the block.
 cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* q, int64_t B,
                               uint8_t* out, float* dist32, float cutoff, int4* items, unsigned int* count, unsigned int cap,
                               uint8_t* overflow, unsigned long long* stats, int cpb, int nt, cudaStream_t s, void* hq = nullptr,
-                              unsigned long long* hq_count = nullptr, unsigned int hq_cap = 0, const FastTuning& tune = FastTuning());
+                              unsigned long long* hq_count = nullptr, unsigned int hq_cap = 0, const FastTuning& tune = FastTuning(),
+                              PmLinkBounds bnd = PmLinkBounds{nullptr, 0});
 
 cudaError_t launch_fast_edges(const PmTablesHdr* T, const PmTablesHdr& h, const double* state, const double* s1, const double* s2,
                               int64_t E, int type, const double* width, double resolution, const int16_t* seq, double* sr, int32_t* n,
                               int64_t* off, unsigned long long* next, uint8_t* out, int4* items, unsigned int* count,
-                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int nt, int n_sm, cudaStream_t s);
+                              unsigned int cap, uint8_t* overflow, unsigned long long* stats, int cpb, int nt, int n_sm, cudaStream_t s,
+                              PmLinkBounds bnd = PmLinkBounds{nullptr, 0});
 
 // ---- differentiable costs (k_grad.cu): FP32 forward + reverse-mode adjoint
 #define PM_GRAD_MAXQ (PM_MAX_CTRL + 8)

@@ -88,13 +88,28 @@ __device__ inline bool self_ok(const TView& v, const DPose* pose) {
   return true;
 }
 
-// IneqConstraintBase::is_valid for one q (primitive.hpp:113-117, :181-189)
-__device__ inline bool is_valid_cfg(const TView& v, const double* state, const double* q) {
+// LinkPositionBoundCst::is_valid_dirty (primitive_link_position_bound.cpp:69-79) of every bound
+// term, on the poses of one configuration.
+__device__ inline bool bounds_ok(const PmLinkBounds& b, const DPose* pose) {
+  for (int k = 0; k < b.n; k++) {
+    const PmPoseTerm& t = b.t[k];
+    const D3& p = pose[t.slot].t;
+    const double x = t.axis == 0 ? p.x : (t.axis == 1 ? p.y : p.z);
+    if (t.has_lb && x < t.lb) return false;
+    if (t.has_ub && x > t.ub) return false;
+  }
+  return true;
+}
+
+// IneqConstraintBase::is_valid for one q (primitive.hpp:113-117, :181-189); with link-position
+// bounds, IneqCompositeCst::is_valid of the collision constraint and those bounds
+// (composite_constraint.hpp:98-105): one update_kintree(q, false), then every member.
+__device__ inline bool is_valid_cfg(const TView& v, const double* state, const double* q, PmLinkBounds bnd = PmLinkBounds{nullptr, 0}) {
   DPose pose[PM_MAX_SLOTS];
   fk64(v.T, state, q, v.T->base_type == PM_BASE_FIXED, pose);
   if (v.T->n_prims > 0 && !ext_ok(v, pose)) return false;
-  if (v.T->n_pairs > 0) return self_ok(v, pose);
-  return true;
+  if (v.T->n_pairs > 0 && !self_ok(v, pose)) return false;
+  return bnd.n == 0 || bounds_ok(bnd, pose);
 }
 
 }  // namespace pmd

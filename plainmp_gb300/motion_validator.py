@@ -10,17 +10,27 @@ from typing import Sequence
 import numpy as np
 
 from ._lib import Batch, check, f64, lib
-from .constraint import SphereCollisionCst
+from .constraint import IneqCompositeCst, SphereCollisionCst
 
 BOX = 0
 EUCLIDEAN = 1
 
 
 class _ValidatorBase:
+    """cst: a SphereCollisionCst, or an IneqCompositeCst of one SphereCollisionCst and
+    LinkPositionBoundCst members (the composite is checked at every waypoint by the fast path)."""
+
     kind = BOX
 
-    def __init__(self, cst: SphereCollisionCst) -> None:
+    def __init__(self, cst) -> None:
         self.cst = cst
+        self._parts = None
+        if isinstance(cst, IneqCompositeCst):
+            self._parts = cst.fused_parts()
+            if self._parts is None:
+                raise TypeError("a composite validator needs one SphereCollisionCst and LinkPositionBoundCst members")
+        elif not isinstance(cst, SphereCollisionCst):
+            raise TypeError(f"expected SphereCollisionCst or IneqCompositeCst, got {type(cst).__name__}")
         self._width = np.zeros(cst.q_dim())
         self._res = 0.0
         self._dev_width = {}  # device -> width tensor, made once so device calls copy nothing from the host
@@ -44,6 +54,8 @@ class _ValidatorBase:
 
     def check_motion_batch(self, S1, S2, return_count: bool = False):
         """Plain FP64 method, one device thread per edge: (E,) uint8."""
+        if self._parts is not None:
+            raise TypeError("the plain edge method takes a SphereCollisionCst; a composite goes through check_motion_fast")
         b1, b2 = self._edges(S1, S2)
         E = b1.shape[0]
         out, optr = b1.empty((E,), np.uint8)
@@ -66,8 +78,15 @@ class _ValidatorBase:
             out, optr = b1.empty((E,), np.uint8)
         w = self._width_arg(b1)
         st = np.zeros(4, dtype=np.int64)
-        check(lib.pmgpu_check_motion_fast(self.cst._h, b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res), optr,
-                                          C.c_void_p(st.ctypes.data) if stats else None, b1.mem, b1.stream))
+        sp = C.c_void_p(st.ctypes.data) if stats else None
+        if self._parts is None:
+            check(lib.pmgpu_check_motion_fast(self.cst._h, b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res), optr, sp, b1.mem,
+                                              b1.stream))
+        else:
+            sph, bnd = self._parts
+            hs = (C.c_void_p * max(len(bnd), 1))(*[c._h for c in bnd])
+            check(lib.pmgpu_composite_check_motion_fast(sph._h, hs, len(bnd), b1.ptr, b2.ptr, E, self.kind, w.ptr, float(self._res),
+                                                        optr, sp, b1.mem, b1.stream))
         if stats:
             return out, {"waypoints": int(st[0]), "rechecked_terms": int(st[1]), "edges": int(st[2])}
         return out
@@ -111,6 +130,8 @@ class _ValidatorBase:
 
     def checkMotion(self, s1, s2) -> bool:  # noqa: N802 (OMPL's name)
         d = self.cst.q_dim()
+        if self._parts is not None:
+            return bool(self.check_motion_fast(f64(s1, (1, d)), f64(s2, (1, d)))[0])
         return bool(self.check_motion_batch(f64(s1, (1, d)), f64(s2, (1, d)))[0])
 
 

@@ -225,6 +225,22 @@ def test_pose_constraint_construction():
     other = KinematicModel(robot.urdf)
     with pytest.raises(RuntimeError, match="same kinematic chain"):
         IneqCompositeCst([sc, LinkPositionBoundCst(other, j, BaseType.FIXED, robot.end_link, 2, lb=0.1)])
+    assert comp.fused_parts() == (sc, [b])
+    assert IneqCompositeCst([sc]).fused_parts() == (sc, [])
+    assert IneqCompositeCst([b]).fused_parts() is None  # no collision constraint: the members' own checks
+    # the fused C entry point checks its members before any device work
+    import ctypes as C
+
+    from plainmp_gb300 import _lib
+
+    q = np.zeros((2, 7))
+    out = np.zeros(2, dtype=np.uint8)
+    for bad, msg in ((c, "inequality"), (LinkPositionBoundCst(other, j, BaseType.FIXED, robot.end_link, 2, lb=0.1), "same kinematic chain"),
+                     (LinkPositionBoundCst(kin, j[:6], BaseType.FIXED, robot.end_link, 2, lb=0.1), "control joints")):
+        hs = (C.c_void_p * 1)(bad._h)
+        rc = _lib.lib.pmgpu_composite_is_valid_fast(sc._h, hs, 1, q.ctypes.data, 2, out.ctypes.data, None, _lib.MEM_HOST, None)
+        assert rc != 0 and msg in _lib.lib.pmgpu_last_error().decode()
+    assert _lib.lib.pmgpu_composite_is_valid_fast(sc._h, None, -1, q.ctypes.data, 2, out.ctypes.data, None, _lib.MEM_HOST, None) != 0
 
 
 def test_sequential_cst_bookkeeping():

@@ -160,3 +160,108 @@ def test_pose_constraint_update_kintree():
         b.update_kintree(q[0], high_accuracy)
         np.testing.assert_array_equal(kin.debug_get_link_pose(robot.end_link), ref)
         np.testing.assert_array_equal(kin.get_joint_positions(kin.get_joint_ids(robot.control_joints)), q[0])
+
+
+def _oracle_bound_ok(oc, om, lid, q, bounds):
+    """LinkPositionBoundCst::is_valid_dirty after update_kintree(q, false) (Taylor sin/cos),
+    every (axis, lb, ub) of `bounds` on link lid."""
+    oc.update_kintree(q, False)
+    p = om.link_pose(lid)
+    return all((lb is None or p[ax] >= lb) and (ub is None or p[ax] <= ub) for ax, lb, ub in bounds)
+
+
+def test_ineq_composite_fused_at_bound_edges(oracle):
+    """The fused composite path (one launch, one FK) against the oracle, with bounds placed exactly
+    on the FP64 link positions of some configurations: those comparisons fall inside the FP32
+    error band and are decided by the FP64 recheck, bit for bit (p == lb passes, the next double
+    above p as lb fails)."""
+    import torch
+
+    robot, scene = W.chain7_robot(), W.chain7_scene()
+    kin, cst, _ = scenes.make_constraint(robot, scene)
+    Q = W.chain7_configs(4096, seed=21)
+    om, oc, _ = oracle.make_constraint(robot, scene)
+    lid = om.link_id(robot.end_link)
+    pz = []
+    for q in Q[:8]:
+        oc.update_kintree(q, False)
+        pz.append(om.link_pose(lid).copy())
+    bounds = [(2, float(pz[0][2]), None),                        # config 0 exactly at lb: passes
+              (0, None, float(pz[1][0])),                        # config 1 exactly at ub: passes
+              (1, float(np.nextafter(pz[2][1], np.inf)), None)]  # config 2 one double below lb: fails
+    mk = [LinkPositionBoundCst(kin, robot.control_joints, BaseType.FIXED, robot.end_link, ax, lb=lb, ub=ub) for ax, lb, ub in bounds]
+    comp = IneqCompositeCst([cst] + mk)
+    assert comp.fused_parts() is not None
+    ref_s = oc.is_valid(Q, threads=8).astype(bool)
+    ref = np.array([s and _oracle_bound_ok(oc, om, lid, q, bounds) for s, q in zip(ref_s, Q)])
+    assert 0 < ref.sum() < len(Q)
+    got, st = comp.is_valid_fast(Q, stats=True)
+    assert np.array_equal(got.astype(bool), ref)
+    assert st["rechecked_terms"] > 0  # the boundary configurations went to the FP64 recheck
+    # the same booleans as the members' own plain checks, and on device tensors
+    plain = cst.is_valid_batch(Q).astype(bool)
+    for b in mk:
+        plain &= b.is_valid_batch(Q).astype(bool)
+    assert np.array_equal(plain, ref)
+    Qd = torch.tensor(Q, device="cuda")
+    assert np.array_equal(comp.is_valid_batch(Qd).cpu().numpy().astype(bool), ref)
+    # the members' order does not matter
+    comp2 = IneqCompositeCst(mk[::-1] + [cst])
+    assert np.array_equal(comp2.is_valid_batch(Q).astype(bool), ref)
+
+
+def _oracle_edge_waypoints(S1, S2, width, seq):
+    """The states checkMotion tests for each edge, in order (motion_validator.cpp:17-79, 89-111):
+    none when the step ratio is infinite, else s2 first, then the interior points in the sequence
+    table's order (or in plain order past 128 tests); interpolation s1 + (s2 - s1) t."""
+    out = []
+    for a, b in zip(S1, S2):
+        d = b - a
+        k = int(np.argmax(np.abs(d) / width))
+        if abs(d[k]) < 1e-6:
+            out.append([])
+            continue
+        r = width[k] / abs(d[k])
+        n_test = int(np.floor(1 / r)) + 2
+        if n_test < seq.shape[0] + 1:
+            ts = [seq[n_test - 1][i] * r for i in range(2, n_test)]
+        else:
+            ts = [i * r for i in range(1, n_test - 1)]
+        out.append([b] + [a + (b - a) * t for t in ts])
+    return out
+
+
+def test_composite_motion_validator(oracle):
+    """checkMotion with a composite (collision + link-position bound) through the fused edge
+    path, against the oracle's composite is_valid at every waypoint the reference would test."""
+    from plainmp_gb300 import BoxMotionValidator
+
+    robot, scene = W.chain7_robot(), W.chain7_scene()
+    kin, cst, _ = scenes.make_constraint(robot, scene)
+    bound = (2, 0.05, None)
+    b = LinkPositionBoundCst(kin, robot.control_joints, BaseType.FIXED, robot.end_link, 2, lb=0.05)
+    comp = IneqCompositeCst([cst, b])
+    s1, s2 = W.chain7_edges(96, seed=4)
+    width = np.full(7, 0.05)
+    mv = BoxMotionValidator(comp, list(width))
+    got = mv.check_motion_fast(s1, s2).astype(bool)
+    om, oc, _ = oracle.make_constraint(robot, scene)
+    lid = om.link_id(robot.end_link)
+    wps = _oracle_edge_waypoints(s1, s2, width, oracle.sequence_table())
+    ref = []
+    for pts in wps:
+        if not pts:
+            ref.append(True)
+            continue
+        P = np.array(pts)
+        ok_s = oc.is_valid(P, threads=8).astype(bool)
+        ref.append(bool(all(s and _oracle_bound_ok(oc, om, lid, p, [bound]) for s, p in zip(ok_s, P))))
+    ref = np.array(ref)
+    assert 0 < ref.sum() < len(ref)
+    assert np.array_equal(got, ref)
+    # the collision constraint alone agrees with the plain edge method; the bound only removes edges
+    alone = BoxMotionValidator(cst, list(width)).check_motion_batch(s1, s2).astype(bool)
+    assert np.all(got <= alone)
+    assert mv.checkMotion(s1[0], s2[0]) == bool(ref[0])
+    with pytest.raises(TypeError):
+        mv.check_motion_batch(s1, s2)
