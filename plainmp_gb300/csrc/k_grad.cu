@@ -36,13 +36,14 @@ struct GSlot {
   float axis[3];
   float lq[4];  // REV: joint origin rotation; STATE: the fixed local rotation
   float lt[3];  // joint origin / fixed local translation
+  int send;     // one past the last slot of this slot's subtree (subtrees are contiguous in slot order)
 };
 struct alignas(16) GSph {  // 32 bytes: one 16-byte and one 8-byte shared-memory load per sphere
   float x, y, z, r;
   int slot, active;  // active: takes part in the ext cost (its group is not self-only)
   int pad0, pad1;
 };
-struct GPrim {
+struct alignas(16) GPrim {  // pos and bound in one 16-byte load
   int kind, aa, cloud, pad;
   float pos[3], bound;  // bound: radius of a sphere around pos containing the primitive (<0: no cull)
   float rot[9];
@@ -52,7 +53,7 @@ constexpr int kSlotF = 33;  // floats of per-unit work per slot (odd: lanes on d
 
 struct Layout {
   int n_slots, n_sph, n_prims, qd, qpad;
-  size_t off_slots, off_sph, off_sbeg, off_prims, off_warp, warp_floats, total;
+  size_t off_slots, off_sph, off_sbeg, off_prims, off_sbnd, off_warp, warp_floats, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -74,6 +75,8 @@ __host__ __device__ inline Layout make_layout(int n_slots, int n_sph, int n_prim
   o = al16(o + sizeof(int) * (n_slots + 1));
   L.off_prims = o;
   o = al16(o + sizeof(GPrim) * n_prims);
+  L.off_sbnd = o;
+  o = al16(o + sizeof(float4) * n_slots);
   L.off_warp = o;
   // per warp: q, grad, target/pose wrench scratch (16), slot work, sphere adjoints (6 each)
   L.warp_floats = (size_t)2 * L.qpad + 16 + (size_t)kSlotF * n_slots + (size_t)6 * n_sph;
@@ -87,6 +90,8 @@ struct Tab {
   const GSph* sph;
   const int* sbeg;
   const GPrim* prim;
+  const float4* sbnd;  // per slot: a sphere in the slot frame containing its active spheres (w < 0: none)
+  bool tree_ok;        // every subtree is the contiguous slot range [i, send) (DFS preorder)
   const PmGridDev* clouds;
   int n_slots, n_sph, n_prims, qd, n_ctrl, base_type;
   float base_q[4], base_t[3];
@@ -158,10 +163,61 @@ __device__ void stage(const PmTablesHdr* T, const double* state, const Layout& L
     }
     pr[i] = g;
   }
+  __syncthreads();
+  // subtree ranges: slot i's subtree is [i, send) when the slots are in DFS preorder (checked)
+  __shared__ int tree_bad;
+  if (threadIdx.x == 0) tree_bad = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < L.n_slots; i += blockDim.x) {
+    int e = i + 1;
+    while (e < L.n_slots) {  // the first later slot outside i's subtree
+      int a = sl[e].parent;
+      while (a > i) a = sl[a].parent;
+      if (a != i) break;
+      e++;
+    }
+    for (int j = e; j < L.n_slots; j++) {  // no later slot may fall back into the subtree
+      int a = sl[j].parent;
+      while (a > i) a = sl[a].parent;
+      if (a == i) tree_bad = 1;
+    }
+    sl[i].send = e;
+  }
+  __syncthreads();
+  t.tree_ok = tree_bad == 0;
+  // per slot: centre = mean of its active spheres' centres, radius = the largest |c_j - centre| + r_j,
+  // widened by 1e-5 relative + 1 um so that it also holds the FP32 sphere centres of the cost
+  float4* bs = (float4*)(smem + L.off_sbnd);
+  for (int i = threadIdx.x; i < L.n_slots; i += blockDim.x) {
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    int n = 0;
+    for (int k = sb[i]; k < sb[i + 1]; k++)
+      if (sp[k].active) {
+        cx += sp[k].x;
+        cy += sp[k].y;
+        cz += sp[k].z;
+        n++;
+      }
+    float R = -1.f;
+    if (n > 0) {
+      cx /= (float)n;
+      cy /= (float)n;
+      cz /= (float)n;
+      R = 0.f;
+      for (int k = sb[i]; k < sb[i + 1]; k++)
+        if (sp[k].active) {
+          const float dx = sp[k].x - cx, dy = sp[k].y - cy, dz = sp[k].z - cz;
+          R = fmaxf(R, sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) + sp[k].r);
+        }
+      R = R * (1.f + 1e-5f) + 1e-6f;
+    }
+    bs[i] = make_float4(cx, cy, cz, R);
+  }
   t.slot = sl;
   t.sph = sp;
   t.sbeg = sb;
   t.prim = pr;
+  t.sbnd = bs;
   t.clouds = pm_at<PmGridDev>(T, T->off_clouds);
   t.n_slots = L.n_slots;
   t.n_sph = L.n_sph;
@@ -243,32 +299,88 @@ __device__ void warp_fk(const Tab& t, const WS& ws, int lane) {
     w[7] = 0.f;
   }
   __syncwarp();
-  if (lane == 0) {
+  // world poses, parents first: the base pose at the root, then T_i = T_parent(i) o local_i
+  auto base_pose = [&](FQ& bq, float bt[3]) {
+    bq = FQ{t.base_q[0], t.base_q[1], t.base_q[2], t.base_q[3]};
+    bt[0] = t.base_t[0];
+    bt[1] = t.base_t[1];
+    bt[2] = t.base_t[2];
+    if (t.base_type == PM_BASE_PLANAR) {
+      const float* qb = ws.q + t.n_ctrl;
+      float sn, cs;
+      sincosf(qb[2] * 0.5f, &sn, &cs);
+      bq = FQ{0.f, 0.f, sn, cs};
+      bt[0] = qb[0];
+      bt[1] = qb[1];
+      bt[2] = 0.f;
+    } else if (t.base_type == PM_BASE_FLOATING) {
+      const float* qb = ws.q + t.n_ctrl;
+      float sr, cr, sp, cp, sy, cy;
+      sincosf(qb[3] * 0.5f, &sr, &cr);
+      sincosf(qb[4] * 0.5f, &sp, &cp);
+      sincosf(qb[5] * 0.5f, &sy, &cy);
+      bq = FQ{sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy, cr * cp * cy + sr * sp * sy};
+      bt[0] = qb[0];
+      bt[1] = qb[1];
+      bt[2] = qb[2];
+    }
+  };
+  if (t.n_slots <= GW) {
+    // one slot per lane, pointer jumping over the slot tree: each step composes the transform
+    // accumulated so far with that of the current ancestor and jumps to the ancestor's ancestor,
+    // so depth d takes ceil(log2(d + 1)) steps (a chain of 8 slots: 3) instead of d serial ones
+    const unsigned FULL = 0xffffffffu;
+    const int i = lane;
+    const bool own = i < t.n_slots;
+    FQ q{0.f, 0.f, 0.f, 1.f};
+    float tr[3] = {0.f, 0.f, 0.f};
+    int anc = -1;
+    if (own) {
+      const float* w = ws.sw + (size_t)i * kSlotF;
+      anc = t.slot[i].parent;
+      if (anc < 0) {
+        base_pose(q, tr);
+      } else {
+        q = w[7] != 0.f ? FQ{0.f, 0.f, 0.f, 1.f} : FQ{w[0], w[1], w[2], w[3]};  // flagged identity, as the serial path
+        tr[0] = w[4];
+        tr[1] = w[5];
+        tr[2] = w[6];
+      }
+    }
+    while (__any_sync(FULL, anc >= 0)) {  // warp-uniform
+      const int src = anc >= 0 ? anc : i;
+      const FQ aq{__shfl_sync(FULL, q.x, src, GW), __shfl_sync(FULL, q.y, src, GW), __shfl_sync(FULL, q.z, src, GW),
+                  __shfl_sync(FULL, q.w, src, GW)};
+      const float at[3] = {__shfl_sync(FULL, tr[0], src, GW), __shfl_sync(FULL, tr[1], src, GW), __shfl_sync(FULL, tr[2], src, GW)};
+      const int aa = __shfl_sync(FULL, anc, src, GW);
+      if (anc >= 0) {
+        float r[3];
+        fqrot(aq, tr, r);
+        tr[0] = at[0] + r[0];
+        tr[1] = at[1] + r[1];
+        tr[2] = at[2] + r[2];
+        q = fqmul(aq, q);
+        anc = aa;
+      }
+    }
+    if (own) {
+      float* w = ws.sw + (size_t)i * kSlotF;
+      w[8] = q.x;
+      w[9] = q.y;
+      w[10] = q.z;
+      w[11] = q.w;
+      w[12] = tr[0];
+      w[13] = tr[1];
+      w[14] = tr[2];
+    }
+  } else if (lane == 0) {
     for (int i = 0; i < t.n_slots; i++) {
       const GSlot& s = t.slot[i];
       float* w = ws.sw + (size_t)i * kSlotF;
       if (s.parent < 0) {
-        FQ bq{t.base_q[0], t.base_q[1], t.base_q[2], t.base_q[3]};
-        float bt[3] = {t.base_t[0], t.base_t[1], t.base_t[2]};
-        if (t.base_type == PM_BASE_PLANAR) {
-          const float* qb = ws.q + t.n_ctrl;
-          float sn, cs;
-          sincosf(qb[2] * 0.5f, &sn, &cs);
-          bq = FQ{0.f, 0.f, sn, cs};
-          bt[0] = qb[0];
-          bt[1] = qb[1];
-          bt[2] = 0.f;
-        } else if (t.base_type == PM_BASE_FLOATING) {
-          const float* qb = ws.q + t.n_ctrl;
-          float sr, cr, sp, cp, sy, cy;
-          sincosf(qb[3] * 0.5f, &sr, &cr);
-          sincosf(qb[4] * 0.5f, &sp, &cp);
-          sincosf(qb[5] * 0.5f, &sy, &cy);
-          bq = FQ{sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy, cr * cp * cy + sr * sp * sy};
-          bt[0] = qb[0];
-          bt[1] = qb[1];
-          bt[2] = qb[2];
-        }
+        FQ bq;
+        float bt[3];
+        base_pose(bq, bt);
         w[8] = bq.x;
         w[9] = bq.y;
         w[10] = bq.z;
@@ -386,11 +498,16 @@ __device__ __forceinline__ float prim_value_grad(const GPrim& P, const float c[3
 
 // d_s of one sphere centre: min over primitives (lower bound below thr) of evaluate - r, with the
 // gradient of the argmin primitive.  +inf (zero gradient) when every primitive is past thr.
-__device__ __forceinline__ float sphere_min_dist(const Tab& t, const float c[3], float r, float thr, float grad[3]) {
+// mask: the primitives its slot's bounding sphere leaves in reach (bit j: primitive j; all primitives
+// beyond 32 are tested).
+__device__ __forceinline__ float sphere_min_dist(const Tab& t, const float c[3], float r, float thr, float grad[3], unsigned mask) {
   float best = INFINITY;
   grad[0] = grad[1] = grad[2] = 0.f;
-  for (int j = 0; j < t.n_prims; j++) {
+  for (int j = t.n_prims <= 32 ? (mask ? __ffs(mask) - 1 : t.n_prims) : 0; j < t.n_prims;) {
     const GPrim& P = t.prim[j];
+    const int jn = j + 1;
+    // the next primitive: the next set bit of the mask (or the next index beyond 32 primitives)
+    j = t.n_prims <= 32 ? ((mask &= mask - 1) ? __ffs(mask) - 1 : t.n_prims) : jn;
     if (P.bound >= 0.f) {
       const float dx = c[0] - P.pos[0], dy = c[1] - P.pos[1], dz = c[2] - P.pos[2];
       const float lb = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - P.bound - r;
@@ -470,8 +587,30 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
       }
     }
   }
-  // spheres
+  // spheres; first, per slot, the primitives its bounding sphere leaves within thr (a sphere's
+  // distance lower bound is at least its slot's), kept in the slot work's word 31
   const float thr = a.mode == MODE_MIN ? a.cutoff : a.margin;
+  for (int i = lane; i < t.n_slots; i += GW) {
+    const float4 b = t.sbnd[i];
+    float* w = ws.sw + (size_t)i * kSlotF;
+    unsigned m = 0;
+    if (b.w >= 0.f && t.n_prims <= 32) {
+      const float* R = w + 16;
+      const float gx = fmaf(R[0], b.x, fmaf(R[1], b.y, fmaf(R[2], b.z, w[12])));
+      const float gy = fmaf(R[3], b.x, fmaf(R[4], b.y, fmaf(R[5], b.z, w[13])));
+      const float gz = fmaf(R[6], b.x, fmaf(R[7], b.y, fmaf(R[8], b.z, w[14])));
+      for (int j = 0; j < t.n_prims; j++) {
+        const GPrim& P = t.prim[j];
+        // keep unless |gc - pos| >= thr + bound + R (squared, with 1e-5 relative to spare)
+        const float sr = thr + P.bound + b.w;
+        const float dx = gx - P.pos[0], dy = gy - P.pos[1], dz = gz - P.pos[2];
+        const bool keep = P.bound < 0.f || (sr > 0.f && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < sr * sr * (1.f + 1e-5f));
+        m |= keep ? 1u << j : 0u;
+      }
+    }
+    w[31] = __uint_as_float(m);
+  }
+  __syncwarp();
   float best_d = INFINITY;
   int best_k = 0x7fffffff;
   float best_g[3] = {0.f, 0.f, 0.f};
@@ -487,7 +626,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
     float g[3] = {0.f, 0.f, 0.f};
     float f[3] = {0.f, 0.f, 0.f};
     if (s.active) {
-      const float d = sphere_min_dist(t, c, s.r, thr, g);
+      const float d = sphere_min_dist(t, c, s.r, thr, g, __float_as_uint(w[31]));
       if (a.mode == MODE_SUM) {
         const float h = fmaxf(a.margin - d, 0.f);
         hsum = fmaf(h, h, hsum);
@@ -572,7 +711,46 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
   }
   for (int j = lane; j < t.qd; j += GW) ws.g[j] = 0.f;
   __syncwarp();
-  if (lane == 0) {  // children first: move each subtree wrench to the parent origin
+  if (t.n_slots <= GW && t.tree_ok) {
+    // subtree totals on the unit's lanes, one slot each: with moments taken about the world origin
+    // (M + o x F) a subtree's wrench is a plain sum, and a subtree is the slot range [i, send), so
+    // an inclusive prefix sum over the lanes gives every total at once; the moment is then moved
+    // back to the slot's origin (M_sub - o x F_sub)
+    const unsigned FULL = 0xffffffffu;
+    const int i = lane;
+    const bool own = i < t.n_slots;
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, o[3] = {0.f, 0.f, 0.f};
+    if (own) {
+      const float* w = ws.sw + (size_t)i * kSlotF;
+      for (int k = 0; k < 3; k++) {
+        o[k] = w[12 + k];
+        v[k] = w[25 + k];
+      }
+      float m[3];
+      cross3(o, v, m);
+      for (int k = 0; k < 3; k++) v[3 + k] = w[28 + k] + m[k];
+    }
+    for (int d = 1; d < GW; d <<= 1)
+      for (int k = 0; k < 6; k++) {
+        const float u = __shfl_up_sync(FULL, v[k], d, GW);
+        if (i >= d) v[k] += u;
+      }
+    const int e = own ? t.slot[i].send - 1 : i;
+    float sub[6];
+    for (int k = 0; k < 6; k++) {
+      const float hi = __shfl_sync(FULL, v[k], e, GW), lo = __shfl_sync(FULL, v[k], i > 0 ? i - 1 : 0, GW);
+      sub[k] = i > 0 ? hi - lo : hi;
+    }
+    if (own) {
+      float* w = ws.sw + (size_t)i * kSlotF;
+      float m[3];
+      cross3(o, sub, m);
+      for (int k = 0; k < 3; k++) {
+        w[25 + k] = sub[k];
+        w[28 + k] = sub[3 + k] - m[k];
+      }
+    }
+  } else if (lane == 0) {  // children first: move each subtree wrench to the parent origin
     for (int i = t.n_slots - 1; i >= 0; i--) {
       const int p = t.slot[i].parent;
       if (p < 0) continue;

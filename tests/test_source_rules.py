@@ -9,8 +9,10 @@ sync points, and later shuffles return values from lanes that run other code.
 The usual way to break this is a conditionally evaluated call: `have && __shfl_sync(...)` or
 `c ? __shfl_sync(...) : x`, or an unbraced `if (c) v = __shfl_sync(...)`. A lane whose condition is
 false skips the call. The rule below rejects a warp intrinsic that is preceded in its own
-statement by `&&`, `||`, `?` or an `if (...)` header. Loops and braced branches whose condition is
-warp-uniform are left to review.
+statement by `&&`, `||`, `?` or an `if (...)` header. A second rule rejects a warp intrinsic
+anywhere inside a braced branch taken by one lane (`if (lane == 0) { ... }`, also `hl`, `sub`,
+`tid`, `threadIdx.x`, `(threadIdx.x & 31)`): the other lanes the mask names never reach it. Loops
+and braced branches whose condition is warp-uniform are left to review.
 """
 import re
 from pathlib import Path
@@ -45,6 +47,36 @@ def conditional_warp_calls(src: str):
     return found
 
 
+_ONE_LANE = re.compile(r"\bif\s*\(\s*(?:lane|hl|sub|tid|threadIdx\.x|\(threadIdx\.x\s*&\s*31\))\s*==\s*0\s*\)\s*\{")
+
+
+def one_lane_warp_calls(src: str):
+    """Line of every warp intrinsic inside a braced `if (<lane> == 0) { ... }` branch."""
+    s = _strip_comments(src)
+    found = []
+    for m in _ONE_LANE.finditer(s):
+        depth, j = 1, m.end()
+        while j < len(s) and depth:
+            depth += {"{": 1, "}": -1}.get(s[j], 0)
+            j += 1
+        for c in _INTRINSIC.finditer(s, m.end(), j):
+            found.append(s.count("\n", 0, c.start()) + 1)
+    return found
+
+
+def test_rule_catches_one_lane_branches():
+    planted = """
+    __device__ void f(int lane, int v, bool need) {
+      if (lane == 0) {
+        atomicAdd(&g, __popc(__ballot_sync(0xffffffffu, need)));   // only lane 0 arrives
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, need);           // fine
+      if ((threadIdx.x & 31) == 0) { if (v) { v = __shfl_sync(0xffffffffu, v, 0); } }
+    }
+    """
+    assert one_lane_warp_calls(planted) == [4, 7]
+
+
 def test_rule_catches_conditional_calls():
     planted = """
     __device__ void f(bool have, int v) {
@@ -65,6 +97,12 @@ def test_warp_intrinsics_are_unconditional(path):
     assert not bad, f"{path.name}: warp intrinsic evaluated conditionally at " + "; ".join(
         f"line {ln}: ...{ctx}" for ln, ctx in bad
     )
+
+
+@pytest.mark.parametrize("path", sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")), ids=lambda p: p.name)
+def test_no_warp_intrinsics_in_one_lane_branches(path):
+    bad = one_lane_warp_calls(path.read_text())
+    assert not bad, f"{path.name}: warp intrinsic inside a one-lane branch at lines {bad}"
 
 
 def test_profile_commands_run_committed_files():
