@@ -265,3 +265,27 @@ def test_composite_motion_validator(oracle):
     assert mv.checkMotion(s1[0], s2[0]) == bool(ref[0])
     with pytest.raises(TypeError):
         mv.check_motion_batch(s1, s2)
+
+
+def test_ineq_composite_fused_bound_beyond_spheres(oracle):
+    """A bound on a link no sphere chain reaches (spheres only on links 1-5, bounds on link7): the
+    link joins the collision constraint's FK slots, and the fused check still equals the oracle's
+    composite, here with a lower and an upper bound on different axes, on a PLANAR base."""
+    r = W.chain7_robot()
+    keep = {"link1", "link2", "link3", "link4", "link5"}
+    robot = W.Robot(r.urdf, r.control_joints, r.end_link, [s for s in r.spheres if s.parent_link_name in keep],
+                    [p for p in r.self_pairs if p[0] in keep and p[1] in keep], base_type="PLANAR")
+    scene = W.chain7_scene()
+    kin, cst, _ = scenes.make_constraint(robot, scene)
+    bounds = [(0, -0.3, None), (2, None, 0.45)]
+    mk = [LinkPositionBoundCst(kin, robot.control_joints, BaseType.PLANAR, "link7", ax, lb=lb, ub=ub) for ax, lb, ub in bounds]
+    comp = IneqCompositeCst([cst] + mk)
+    Q = configs("PLANAR", 2048, 31)
+    om, oc, _ = oracle.make_constraint(robot, scene)
+    lid = om.link_id("link7")
+    ref_s = oc.is_valid(Q, threads=8).astype(bool)
+    ref = np.array([s and _oracle_bound_ok(oc, om, lid, q, bounds) for s, q in zip(ref_s, Q)])
+    assert 0 < ref.sum() < len(Q) and ref.sum() < ref_s.sum()
+    assert np.array_equal(comp.is_valid_batch(Q).astype(bool), ref)
+    # the collision constraint alone is unchanged by the extra slots
+    assert np.array_equal(cst.is_valid_fast(Q).astype(bool), ref_s)
