@@ -427,6 +427,7 @@ struct HostSdf {
       return;
     }
     if (kind == PM_SDF_GROUND) fail(PMGPU_ERR_RUNTIME, "GroundSDF does not support translation");
+    // the reference's CloudSDF raises this very message (collision/primitive_sdf.hpp:584-607)
     if (kind == PM_SDF_CLOUD) fail(PMGPU_ERR_RUNTIME, "TODO: Not implemented yet");
     for (int a = 0; a < 3; a++) pos[a] += t[a];
     update_aabb();

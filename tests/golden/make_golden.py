@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference mounted (default /root/reference):
+Run where the reference checkout is available, its root given as the argument or in PLAINMP_REF:
 
     python tests/golden/make_golden.py [reference_root]
 
