@@ -2,16 +2,21 @@
 // IK (cost, gradient, and whole gradient-descent runs in one launch) and trajectory smoothing
 // with the collision hinge (FK recomputed per waypoint in the backward pass, nothing stored).
 //
-// One warp per unit (an IK problem or a trajectory waypoint).  Per evaluation:
-//   1. FK: lanes build the slots' local transforms (sincosf), lane 0 composes them parents-first,
-//      lanes turn the world quaternions into rotation matrices;
-//   2. spheres: each lane takes spheres (ordered by slot) and computes d_s = min over primitives
+// A unit of GW lanes per IK problem (16: two problems per warp) or per trajectory waypoint (a warp).
+// Per evaluation:
+//   1. FK: lanes build the slots' local transforms (sincosf); with a slot per lane, pointer jumping
+//      over the slot tree composes the world poses in ceil(log2(depth + 1)) steps (else the unit's
+//      first lane composes them parents-first); lanes turn the world quaternions into rotation
+//      matrices;
+//   2. spheres: per slot, the primitives the slot's bounding sphere leaves within the threshold;
+//      then each lane takes spheres (ordered by slot) and computes d_s = min over those primitives
 //      of evaluate(c) - r (the SphereCollisionCst ext-row value, primitive_sphere_collision.cpp:
 //      256-322), skipping primitives whose bounding-sphere lower bound is already past the
 //      threshold, with the analytic SDF gradient of the argmin primitive;
 //   3. adjoint: the cost's gradient with respect to each sphere centre is a force at the centre;
-//      forces and moments are summed per slot, then accumulated up the tree (children first), and
-//      a revolute joint's derivative is its world axis dotted with the moment about its origin
+//      forces and moments are summed per slot, then over each subtree (a prefix sum over the lanes
+//      in DFS order, moments about the world origin; else children first on one lane), and a
+//      revolute joint's derivative is its world axis dotted with the moment about its origin
 //      (prismatic: with the force).  This is the transpose of the attached-point Jacobian of
 //      algorithm.cpp:346-380 applied to every sphere at once, in O(slots + spheres).
 // The pose term ||p - p*||^2 + w_rot ||log(R*^T R)||^2 adds a force 2 w_pos (p - p*) at the pose
@@ -29,7 +34,7 @@ using namespace pmd;
 
 namespace {
 
-constexpr int kNW = 8;  // warps (units in flight) per block
+constexpr int kNW = 8;  // warps per block
 
 struct GSlot {
   int parent, mode, qcol, lid;
