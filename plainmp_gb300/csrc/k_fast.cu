@@ -1522,7 +1522,8 @@ __device__ __forceinline__ void atomic_min_float(float* a, float v) {
 }
 
 // The hard cloud queries of a k_fast_valid launch with distances, two per warp (one per half) over the
-// whole queue (no per-block barrier), the next pair's field records read before the current searches.
+// whole queue (no per-block barrier), the next pair's field records read before the current searches
+// from query points read one iteration earlier still (so that read is not waited for).
 // Same arithmetic as the in-block answer: the distance goes into dist32 by an exact minimum, a certain
 // collision clears the configuration, an uncertain one goes to the recheck queue.  A query whose cell
 // has no list takes the whole warp's search (warp_nearest32) after the pair's list scans.
@@ -1536,15 +1537,26 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
   const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   int64_t k = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
-  auto record = [&](int64_t i) {  // the half's query i
-    if (i >= n) return make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
-    const HardQuery h = hq[i];
-    return field_corner_record(v.C[v.P[(h.b.y >> 16) & 0x7fff].cloud], h.a.x, h.a.y, h.a.z, hl);
+  const float4 none = make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
+  auto point = [&](int64_t i, int& py) {  // the half's query i: its point and packed indices
+    py = 0;
+    if (i >= n) return make_float4(0.f, 0.f, 0.f, 0.f);
+    py = hq[i].b.y;
+    return hq[i].a;
   };
-  float4 rec = record(k + half);
+  auto record = [&](int64_t i, const float4& qa, int py) {  // field records of query i at point qa
+    if (i >= n) return none;
+    return field_corner_record(v.C[v.P[(py >> 16) & 0x7fff].cloud], qa.x, qa.y, qa.z, hl);
+  };
+  int py0, py1;
+  const float4 qa0 = point(k + half, py0);
+  float4 rec = record(k + half, qa0, py0);
+  float4 qa1 = point(k + 2 * nw + half, py1);  // the next query's point, one iteration ahead
   while (k < n) {  // warp-uniform
     const int64_t kn = k + 2 * nw;
-    const float4 rec_n = record(kn + half);
+    int py2;
+    const float4 qa2 = point(kn + 2 * nw + half, py2);  // issued now, used next iteration
+    const float4 rec_n = record(kn + half, qa1, py1);
     const int64_t i = k + half;
     const bool have = i < n;  // the same on the half's lanes
     HardQuery h;
@@ -1603,6 +1615,8 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
     }
     k = kn;
     rec = rec_n;
+    qa1 = qa2;
+    py1 = py2;
   }
 }
 
