@@ -432,3 +432,28 @@ def test_fast_refuses_tables_beyond_the_queue_records():
     assert cst.is_valid_batch(Q).all()
     with pytest.raises(ValueError, match="32767 primitives"):
         cst.is_valid_fast(Q)
+
+
+def test_fast_single_calls(chain, dual):
+    """One state or one edge per host-memory call, as OMPL's callbacks call, many calls in a row
+    through the same staging buffers: every answer equals the oracle's (validity, edges) or the
+    plain FP64 distances within DIST_TOL."""
+    (_, cst, _), (_, oc, _) = chain
+    Q = W.chain7_configs(40, seed=91)
+    ref = oc.is_valid(Q).astype(bool)
+    got = np.array([bool(cst.is_valid_fast(q[None])[0]) for q in Q])
+    assert np.array_equal(got, ref) and 0 < ref.sum() < len(Q)
+    s1, s2 = W.chain7_edges(24, seed=92, max_waypoints=6)
+    mv = BoxMotionValidator(cst, [0.05] * 7)
+    e_ref = oc.check_motion(s1, s2, 0, [0.05] * 7)[0].astype(bool)
+    e_got = np.array([bool(mv.check_motion_fast(a[None], b[None])[0]) for a, b in zip(s1, s2)])
+    assert np.array_equal(e_got, e_ref) and 0 < e_ref.sum() < len(e_ref)
+    # two states per call, with distances, on the cloud scene
+    (_, cst2, _), (_, oc2, _) = dual
+    Q2 = W.dualarm_configs(30, seed=93)
+    ref2 = oc2.is_valid(Q2).astype(bool)
+    d_ref = np.minimum(cst2.sphere_distances(Q2), CUTOFF)
+    for k in range(0, len(Q2), 2):
+        ok, d = cst2.is_valid_fast(Q2[k:k + 2], distances=True)
+        assert np.array_equal(ok.astype(bool), ref2[k:k + 2])
+        assert np.abs(d.astype(np.float64) - d_ref[k:k + 2]).max() < DIST_TOL
