@@ -353,51 +353,4 @@ __device__ __forceinline__ float point_d2_32(const PmGridDev& G, int idx, float 
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
-// Lower bound (FP32, conservative by 4 um) on the distance from q to any cloud point, from the
-// block distance field alone: 0 when q is outside the grid or near an occupied block.
-__device__ __forceinline__ float grid_lower_bound32(const PmGridDev& G, float qx, float qy, float qz) {
-  if (G.n_points <= 0) return INFINITY;
-  const float inv = G.inv_blk32;
-  const float qa[3] = {qx, qy, qz};
-  const float oa[3] = {G.o32[0], G.o32[1], G.o32[2]};
-  const int nb[3] = {G.nbx, G.nby, G.nbz};
-  int cb[3];
-  for (int a = 0; a < 3; a++) {
-    float f = floorf((qa[a] - oa[a]) * inv);
-    if (!(f >= 0.f && f <= (float)(nb[a] - 1))) return 0.f;
-    cb[a] = (int)f;
-  }
-  const int k0 = __ldg(G.edf + cb[0] + nb[0] * (cb[1] + nb[1] * cb[2]));
-  return k0 >= 2 ? fmaxf((float)(k0 - 1) * G.blk32 - 4e-6f, 0.f) : 0.f;
-}
-
-// Lower bound on the distance from q to any point: inside the grid, the Euclidean distance from
-// q's fine cell to the nearest occupied fine cell (box to box); outside it, the distance to the
-// box of the points (CloudSDF's AABB shrunk by its radius).  4 um below the exact bound, which
-// covers the FP32 cell assignment of q.
-__device__ __forceinline__ float grid_cell_lower_bound32(const PmGridDev& G, float qx, float qy, float qz) {
-  if (G.n_points <= 0) return INFINITY;
-  const float inv = G.inv_cell32;
-  const float qa[3] = {qx, qy, qz};
-  const float oa[3] = {G.o32[0], G.o32[1], G.o32[2]};
-  const int nc[3] = {G.nbx * PM_GRID_B, G.nby * PM_GRID_B, G.nbz * PM_GRID_B};
-  int cc[3];
-  bool inside = true;
-  for (int a = 0; a < 3; a++) {
-    float f = floorf((qa[a] - oa[a]) * inv);
-    if (!(f >= 0.f && f <= (float)(nc[a] - 1))) inside = false;
-    cc[a] = (int)f;
-  }
-  if (!inside) {
-    float d2 = 0.f;
-    for (int a = 0; a < 3; a++) {
-      const float lo = G.box_lo32[a], hi = G.box_hi32[a];
-      const float gap = fmaxf(fmaxf(lo - qa[a], qa[a] - hi), 0.f);
-      d2 = fmaf(gap, gap, d2);
-    }
-    return fmaxf(sqrtf(d2) * (1.0f - 1e-6f) - 4e-6f, 0.f);
-  }
-  return fmaxf(__ldg(G.cell_lb + cc[0] + nc[0] * (cc[1] + nc[1] * cc[2])) - 4e-6f, 0.f);
-}
-
 }  // namespace pmd

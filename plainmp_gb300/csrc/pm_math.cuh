@@ -29,7 +29,6 @@ struct DM3 {
   double m[9];  // row-major
 };
 
-__device__ __forceinline__ D3 d3(double x, double y, double z) { return D3{x, y, z}; }
 __device__ __forceinline__ D3 add(const D3& a, const D3& b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ D3 sub(const D3& a, const D3& b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ double dot(const D3& a, const D3& b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
@@ -38,7 +37,6 @@ __device__ __forceinline__ double nrm(const D3& a) { return sqrt(sqn(a)); }
 __device__ __forceinline__ D3 cross(const D3& a, const D3& b) {
   return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
-__device__ __forceinline__ double comp(const D3& a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 
 // quaternion product a*b (transform.hpp:60, algorithm.cpp:147)
 __device__ __forceinline__ DQ qmul(const DQ& a, const DQ& b) {
