@@ -715,6 +715,65 @@ __device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, dou
     return sb * sb * (1.0f + 1e-6f);
   };
   float t32 = thr(best);
+  // warp minimum of (best, bidx); best >= 0, so its bits order like its value
+  auto warp_min = [&]() {
+    long long bb = __double_as_longlong(best);
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ob = __shfl_xor_sync(FULL, bb, o);
+      const int oi = __shfl_xor_sync(FULL, bidx, o);
+      if (ob < bb || (ob == bb && oi >= 0 && (bidx < 0 || oi < bidx))) {
+        bb = ob;
+        bidx = oi;
+      }
+    }
+    best = __longlong_as_double(bb);
+    t32 = thr(best);
+  };
+  // Where q's fine cell has a cell list (every occupied cell that can hold q's nearest point, nearest
+  // first), the warp scans it 32 entries at a time: an entry whose stored lower bound reaches the
+  // FP32 threshold ends the scan, the others are tested by their box, and the points of each
+  // surviving cell are split over the lanes (FP32 prefilter, then the exact FP64 distance).
+  int2 rng;
+  if (cell_list_of(G, qx, qy, qz, rng)) {  // the same on every lane
+    const float unit = G.cell32 * (1.0f / (float)PM_CL_UNITS);
+    for (int base = rng.x; base < rng.y; base += 32) {  // warp-uniform
+      const int k = base + lane;
+      bool beyond = true;  // this entry, and (sorted) every later one, lies beyond the best
+      int2 pr = make_int2(0, 0);
+      if (k < rng.y) {
+        const uint32_t e = __ldg(G.cl_ent + k);
+        const float lbd = (float)(e >> 24) * unit;
+        beyond = lbd * lbd * (1.0f - 1e-5f) >= t32;
+        if (!beyond) {
+          const int o = (int)(e & 0xffffffu);
+          const float4 lo = __ldg(G.cell_rec + 2 * o), hi = __ldg(G.cell_rec + 2 * o + 1);
+          const float gx = gap32(qx, lo.x, hi.x), gy = gap32(qy, lo.y, hi.y), gz = gap32(qz, lo.z, hi.z);
+          if (!(fmaf(gx, gx, fmaf(gy, gy, gz * gz)) > t32)) pr = make_int2(__float_as_int(lo.w), __float_as_int(hi.w));
+        }
+      }
+      const bool stop = __shfl_sync(FULL, beyond ? 1 : 0, 31) != 0;
+      for (unsigned bal = __ballot_sync(FULL, pr.y > pr.x); bal != 0; bal &= bal - 1) {  // warp-uniform
+        const int src = __ffs(bal) - 1;
+        const int p0 = __shfl_sync(FULL, pr.x, src), p1 = __shfl_sync(FULL, pr.y, src);
+        for (int pi = p0 + lane; pi < p1; pi += 32) {
+          const float4 pt = __ldg(G.p32 + pi);
+          const float ex = pt.x - qx, ey = pt.y - qy, ez = pt.z - qz;
+          if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > t32) continue;
+          const D3 d{G.px[pi] - q.x, G.py[pi] - q.y, G.pz[pi] - q.z};
+          const double d2 = d.x * d.x + (d.y * d.y + d.z * d.z);
+          if (d2 < best || (d2 == best && bidx >= 0 && pi < bidx)) {
+            best = d2;
+            bidx = pi;
+          }
+        }
+      }
+      warp_min();
+      if (stop) break;
+    }
+    r.d2 = best;
+    r.idx = bidx;
+    return r;
+  }
   const float reach = sqrtf((float)maxd2) * (1.0f + 1e-6f);
   const float qa[3] = {qx, qy, qz};
   const int nb[3] = {G.nbx, G.nby, G.nbz};
@@ -765,18 +824,7 @@ __device__ inline NNResult64 warp_nearest64(const PmGridDev& G, const D3& q, dou
           }
         }
       }
-      // warp minimum; best >= 0, so its bits order like its value
-      long long bb = __double_as_longlong(best);
-      for (int o = 16; o > 0; o >>= 1) {
-        const long long ob = __shfl_xor_sync(FULL, bb, o);
-        const int oi = __shfl_xor_sync(FULL, bidx, o);
-        if (ob < bb || (ob == bb && oi >= 0 && (bidx < 0 || oi < bidx))) {
-          bb = ob;
-          bidx = oi;
-        }
-      }
-      best = __longlong_as_double(bb);
-      t32 = thr(best);
+      warp_min();
     }
   }
   r.d2 = best;
