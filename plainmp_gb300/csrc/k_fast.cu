@@ -1575,6 +1575,9 @@ __device__ __forceinline__ void atomic_min_float(float* a, float v) {
 // Same arithmetic as the in-block answer: the distance goes into dist32 by an exact minimum, a certain
 // collision clears the configuration, an uncertain one goes to the recheck queue.  A query whose cell
 // has no list takes the whole warp's search (warp_nearest32) after the pair's list scans.
+// Register budget (64 at 4 blocks of 256 per SM): 32-bit queue indices (the launch allows at most 2^30
+// entries), and only the point, reach and cloud held across the search; the fields the result needs are
+// read again after it (an L1 hit).  With the whole record held, the kernel spilled and ran 6 % slower.
 template <class Src>
 __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __restrict__ T, const HardQuery* __restrict__ hq,
                                                          float* __restrict__ dist32, Src src, Scratch scr) {
@@ -1582,17 +1585,17 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
   const int ns = T->n_spheres;
-  const int64_t n = (int64_t)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t k = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
+  const int n = (int)min(*scr.hq_count, (unsigned long long)scr.hq_cap);
+  const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+  int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;  // the warp's pair: k (half 0), k + 1 (half 1)
   const float4 none = make_float4(__int_as_float(-1), __int_as_float(-1), 0.f, __int_as_float(-1));
-  auto point = [&](int64_t i, int& py) {  // the half's query i: its point and packed indices
+  auto point = [&](int i, int& py) {  // the half's query i: its point and packed indices
     py = 0;
     if (i >= n) return make_float4(0.f, 0.f, 0.f, 0.f);
     py = hq[i].b.y;
     return hq[i].a;
   };
-  auto record = [&](int64_t i, const float4& qa, int py) {  // field records of query i at point qa
+  auto record = [&](int i, const float4& qa, int py) {  // field records of query i at point qa
     if (i >= n) return none;
     return field_corner_record(v.C[v.P[(py >> 16) & 0x7fff].cloud], qa.x, qa.y, qa.z, hl);
   };
@@ -1601,22 +1604,20 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
   float4 rec = record(k + half, qa0, py0);
   float4 qa1 = point(k + 2 * nw + half, py1);  // the next query's point, one iteration ahead
   while (k < n) {  // warp-uniform
-    const int64_t kn = k + 2 * nw;
+    const int kn = k + 2 * nw;
     int py2;
     const float4 qa2 = point(kn + 2 * nw + half, py2);  // issued now, used next iteration
     const float4 rec_n = record(kn + half, qa1, py1);
-    const int64_t i = k + half;
+    const int i = k + half;
     const bool have = i < n;  // the same on the half's lanes
-    HardQuery h;
-    h.a = make_float4(0.f, 0.f, 0.f, 0.f);
-    h.b = make_int4(0, 0, 0, 0);
-    if (have) h = hq[i];
-    const int cfg = h.b.x, si = h.b.y & 0xffff, prim = (h.b.y >> 16) & 0x7fff;
-    const bool check = h.b.y < 0;
-    const float ek = __int_as_float(h.b.z);
-    const float qx = h.a.x, qy = h.a.y, qz = h.a.z, reach = h.a.w;
-    const PmPrim& Pp = v.P[prim];
-    const int cloud = have ? Pp.cloud : 0;  // a half past the end reads cloud 0's constants only
+    float4 ha = make_float4(0.f, 0.f, 0.f, 0.f);
+    int hy = 0;
+    if (have) {
+      ha = hq[i].a;
+      hy = hq[i].b.y;
+    }
+    const float qx = ha.x, qy = ha.y, qz = ha.z, reach = ha.w;
+    const int cloud = have ? v.P[(hy >> 16) & 0x7fff].cloud : 0;  // a half past the end reads cloud 0's constants only
     const FieldStart start = field_corner_candidate(rec, qx, qy, qz, 16);
     const float maxd2 = reach * reach;
     float best = start.nn.d2 < maxd2 ? start.nn.d2 : maxd2;
@@ -1638,8 +1639,12 @@ __global__ void __launch_bounds__(256, 4) k_hard_queries(const PmTablesHdr* __re
         }
       }
     }
-    if (have && hl == 0) {
-      const float pa = (float)Pp.a, sr = (float)v.sr[si];
+    if (have && hl == 0) {  // the query's remaining fields, read again after the search
+      const int4 hb = hq[i].b;
+      const int cfg = hb.x, si = hb.y & 0xffff, prim = (hb.y >> 16) & 0x7fff;
+      const bool check = hb.y < 0;
+      const float ek = __int_as_float(hb.z);
+      const float pa = (float)v.P[prim].a, sr = (float)v.sr[si];
       float g, sd, mag;
       if (bidx < 0) {
         g = reach - pa - sr;
@@ -1918,7 +1923,9 @@ cudaError_t launch_fast_valid(const PmTablesHdr* T, const PmTablesHdr& h, const 
   if (B <= 0) return cudaSuccess;
   if (!fast_table_sizes_ok(h)) return cudaErrorInvalidConfiguration;
   // (hard-query entries hold 32-bit configuration indices)
-  const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && h.n_clouds > 0 && B <= 0x7fffffffLL;
+  // k_hard_queries indexes its queue in 32 bits: at most 2^30 entries
+  const bool split = dist32 != nullptr && hq != nullptr && hq_count != nullptr && hq_cap > 0 && hq_cap <= (1u << 30) &&
+                     h.n_clouds > 0 && B <= 0x7fffffffLL;
   Scratch scr{items, count, cap, overflow, stats, split ? static_cast<HardQuery*>(hq) : nullptr, split ? hq_count : nullptr,
               split ? hq_cap : 0u, tune.sphere_tile_log2, bnd};
   size_t sm = fast_smem_bytes(h, cpb, dist32 != nullptr);
