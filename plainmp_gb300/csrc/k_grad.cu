@@ -56,8 +56,12 @@ struct alignas(16) GPrim {  // pos and bound in one 16-byte load
 };
 constexpr int kSlotF = 33;  // floats of per-unit work per slot (odd: lanes on different slots use different banks)
 
+// Passed by value as a kernel argument: its fields are read from parameter space wherever they are used,
+// so the header values copied here (n_ctrl, base_type, off_clouds: set by the launcher from the host
+// copy of the header) hold no registers across the cost (the IK kernel spills at its 64 registers).
 struct Layout {
-  int n_slots, n_sph, n_prims, qd, qpad;
+  int n_slots, n_sph, n_prims, qd, qpad, n_ctrl, base_type;
+  int64_t off_clouds;
   size_t off_slots, off_sph, off_sbeg, off_prims, off_sbnd, off_warp, warp_floats, total;
 };
 
@@ -96,11 +100,12 @@ struct Tab {
   const int* sbeg;
   const GPrim* prim;
   const float4* sbnd;  // per slot: a sphere in the slot frame containing its active spheres (w < 0: none)
-  bool tree_ok;        // every subtree is the contiguous slot range [i, send) (DFS preorder)
   const PmGridDev* clouds;
   int n_slots, n_sph, n_prims, qd, n_ctrl, base_type;
-  float base_q[4], base_t[3];
 };
+// the fixed base pose ([0..3] quaternion, [4..6] translation) and the subtree-range flag of the block
+__shared__ float g_base_pose[8];
+__shared__ int g_tree_bad;
 
 // Stage the constraint tables into shared memory in FP32 (once per block).
 __device__ void stage(const PmTablesHdr* T, const double* state, const Layout& L, char* smem, Tab& t) {
@@ -170,8 +175,7 @@ __device__ void stage(const PmTablesHdr* T, const double* state, const Layout& L
   }
   __syncthreads();
   // subtree ranges: slot i's subtree is [i, send) when the slots are in DFS preorder (checked)
-  __shared__ int tree_bad;
-  if (threadIdx.x == 0) tree_bad = 0;
+  if (threadIdx.x == 0) g_tree_bad = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < L.n_slots; i += blockDim.x) {
     int e = i + 1;
@@ -184,12 +188,11 @@ __device__ void stage(const PmTablesHdr* T, const double* state, const Layout& L
     for (int j = e; j < L.n_slots; j++) {  // no later slot may fall back into the subtree
       int a = sl[j].parent;
       while (a > i) a = sl[a].parent;
-      if (a == i) tree_bad = 1;
+      if (a == i) g_tree_bad = 1;
     }
     sl[i].send = e;
   }
   __syncthreads();
-  t.tree_ok = tree_bad == 0;
   // per slot: centre = mean of its active spheres' centres, radius = the largest |c_j - centre| + r_j,
   // widened by 1e-5 relative + 1 um so that it also holds the FP32 sphere centres of the cost
   float4* bs = (float4*)(smem + L.off_sbnd);
@@ -223,16 +226,15 @@ __device__ void stage(const PmTablesHdr* T, const double* state, const Layout& L
   t.sbeg = sb;
   t.prim = pr;
   t.sbnd = bs;
-  t.clouds = pm_at<PmGridDev>(T, T->off_clouds);
+  t.clouds = pm_at<PmGridDev>(T, L.off_clouds);
   t.n_slots = L.n_slots;
   t.n_sph = L.n_sph;
   t.n_prims = L.n_prims;
   t.qd = L.qd;
-  t.n_ctrl = T->n_ctrl;
-  t.base_type = T->base_type;
+  t.n_ctrl = L.n_ctrl;
+  t.base_type = L.base_type;
   const double* b = state + (int64_t)PM_STATE_BASE_ROW * PM_STATE_STRIDE;
-  for (int k = 0; k < 4; k++) t.base_q[k] = (float)b[k];
-  for (int k = 0; k < 3; k++) t.base_t[k] = (float)b[4 + k];
+  if (threadIdx.x < 7) g_base_pose[threadIdx.x] = (float)b[threadIdx.x];
   __syncthreads();
 }
 
@@ -306,10 +308,10 @@ __device__ void warp_fk(const Tab& t, const WS& ws, int lane) {
   __syncwarp();
   // world poses, parents first: the base pose at the root, then T_i = T_parent(i) o local_i
   auto base_pose = [&](FQ& bq, float bt[3]) {
-    bq = FQ{t.base_q[0], t.base_q[1], t.base_q[2], t.base_q[3]};
-    bt[0] = t.base_t[0];
-    bt[1] = t.base_t[1];
-    bt[2] = t.base_t[2];
+    bq = FQ{g_base_pose[0], g_base_pose[1], g_base_pose[2], g_base_pose[3]};
+    bt[0] = g_base_pose[4];
+    bt[1] = g_base_pose[5];
+    bt[2] = g_base_pose[6];
     if (t.base_type == PM_BASE_PLANAR) {
       const float* qb = ws.q + t.n_ctrl;
       float sn, cs;
@@ -716,7 +718,7 @@ __device__ float warp_cost(const Tab& t, const CostArgs& a, const WS& ws, const 
   }
   for (int j = lane; j < t.qd; j += GW) ws.g[j] = 0.f;
   __syncwarp();
-  if (t.n_slots <= GW && t.tree_ok) {
+  if (t.n_slots <= GW && g_tree_bad == 0) {
     // subtree totals on the unit's lanes, one slot each: with moments taken about the world origin
     // (M + o x F) a subtree's wrench is a plain sum, and a subtree is the slot range [i, send), so
     // an inclusive prefix sum over the lanes gives every total at once; the moment is then moved
@@ -1004,7 +1006,10 @@ cudaError_t launch_ik_cost(const PmTablesHdr* T, const PmTablesHdr& h, const dou
                            const float* target, int64_t B, float* cost, float* grad, float* hist, cudaStream_t s) {
   if (B <= 0) return cudaSuccess;
   constexpr int GW = kIkGW, groups = kNW * (32 / GW);
-  const Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim, groups);
+  Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim, groups);
+  L.n_ctrl = h.n_ctrl;
+  L.base_type = h.base_type;
+  L.off_clouds = h.off_clouds;
   const CostArgs a = to_args(g, h.q_dim);
   if (grad || g.steps > 0) {
     auto fn = k_ik_cost<true, GW>;
@@ -1027,7 +1032,10 @@ cudaError_t launch_traj_cost(const PmTablesHdr* T, const PmTablesHdr& h, const d
                              cudaStream_t s) {
   if (n_traj <= 0) return cudaSuccess;
   constexpr int GW = kTrajGW, groups = kNW * (32 / GW);
-  const Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim, groups);
+  Layout L = make_layout(h.n_slots, h.n_spheres, h.n_prims, h.q_dim, groups);
+  L.n_ctrl = h.n_ctrl;
+  L.base_type = h.base_type;
+  L.off_clouds = h.off_clouds;
   const CostArgs a = to_args(g, h.q_dim);
   if (n_wp > 0) {
     if (grad) {
